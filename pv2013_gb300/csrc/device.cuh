@@ -1,0 +1,151 @@
+// Device-side definitions shared by the CUDA translation units.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <cuda_bf16.h>
+
+#include "lbm_gb300.h"
+
+namespace lbm {
+
+// ---------------------------------------------------------------------------
+// Lattice tables (LatticeModel.cpp:51-151 for D3Q19 with the rest population
+// at index 18; :208-334 for D3Q27 with the rest population at index 0).
+template <int Q> struct Lat;
+
+template <> struct Lat<19> {
+    static constexpr int Q = 19;
+    static constexpr int REST = 18;
+    // direction index excluded from bounce-back (ApplyWallBc loops dir = 1..Q-1,
+    // Simulation.cpp:1361): population opp(0) = 1 is never bounced back.
+    static constexpr int NO_BB_POP = 1;
+    __host__ __device__ static constexpr int cx(int q) {
+        constexpr int v[19] = {1, -1, 0, 0, 0, 0, 1, 1, 1, 1, -1, -1, -1, -1, 0, 0, 0, 0, 0};
+        return v[q];
+    }
+    __host__ __device__ static constexpr int cy(int q) {
+        constexpr int v[19] = {0, 0, 1, -1, 0, 0, 1, -1, 0, 0, 1, -1, 0, 0, 1, 1, -1, -1, 0};
+        return v[q];
+    }
+    __host__ __device__ static constexpr int cz(int q) {
+        constexpr int v[19] = {0, 0, 0, 0, 1, -1, 0, 0, 1, -1, 0, 0, 1, -1, 1, -1, 1, -1, 0};
+        return v[q];
+    }
+    __host__ __device__ static constexpr int opp(int q) {
+        constexpr int v[19] = {1, 0, 3, 2, 5, 4, 11, 10, 13, 12, 7, 6, 9, 8, 17, 16, 15, 14, 18};
+        return v[q];
+    }
+    // weights exactly as the reference's double expressions 2/36, 1/36, 12/36
+    __host__ __device__ static constexpr double w(int q) {
+        return q < 6 ? 2.0 / 36.0 : (q < 18 ? 1.0 / 36.0 : 12.0 / 36.0);
+    }
+};
+
+template <> struct Lat<27> {
+    static constexpr int Q = 27;
+    static constexpr int REST = 0;
+    static constexpr int NO_BB_POP = -1;   // ApplyWallBc dir = 1..26 covers every moving direction
+    __host__ __device__ static constexpr int cx(int q) {
+        constexpr int v[27] = {0, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1, 1, -1, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 1, -1, 1, -1};
+        return v[q];
+    }
+    __host__ __device__ static constexpr int cy(int q) {
+        constexpr int v[27] = {0, 0, 0, 1, -1, 0, 0, 1, -1, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1, 1, -1, 1, -1, -1, 1, -1, 1};
+        return v[q];
+    }
+    __host__ __device__ static constexpr int cz(int q) {
+        constexpr int v[27] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 0, 0, 1, 1, -1, -1, 1, -1, 1, -1, 1, -1, -1, 1, 1, -1, -1, 1};
+        return v[q];
+    }
+    __host__ __device__ static constexpr int opp(int q) {
+        constexpr int v[27] = {0, 2, 1, 4, 3, 6, 5, 10, 9, 8, 7, 14, 13, 12, 11, 18, 17, 16, 15, 20, 19, 22, 21, 24, 23, 26, 25};
+        return v[q];
+    }
+    __host__ __device__ static constexpr double w(int q) {
+        return q == 0 ? 8.0 / 27.0 : (q < 7 ? 2.0 / 27.0 : (q < 19 ? 1.0 / 54.0 : 1.0 / 216.0));
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Run-table lattice: fluid nodes are numbered in x-major order (z fastest);
+// each z-run of a grid column is cut into chunks of at most 32 nodes, one warp
+// per chunk.  For the nine columns (i+di, j+dj), di,dj in {-1,0,1}, a chunk
+// holds a fluid bit mask over the window k0-1 .. k0+32 (bit b <-> k0-1+b) and
+// the node id of the lowest fluid point of that window, so the node id of any
+// neighbour of lane t is base + popcount(mask below its bit).
+struct __align__(128) Chunk {
+    int32_t n0;        // node id of lane 0
+    uint32_t len_inst; // bits 0-7: number of nodes (1..32); bits 8-31: instance
+    uint32_t wmask;    // lanes that are wall nodes (bounce-back)
+    uint32_t zmask;    // lanes that carry a Zou-He boundary condition
+    int32_t zslot0;    // Zou-He slot of the first such lane
+    int32_t base[9];   // column (di,dj) -> index (di+1)*3 + (dj+1)
+    uint64_t mask[9];
+};
+static_assert(sizeof(Chunk) == 128, "chunk descriptor is one 128-byte line");
+
+// Zou-He slot of one boundary node.
+struct ZSlot {
+    double profile;    // inlet profile factor (1 for outlets)
+    int32_t list;      // global list index (instance lists concatenated)
+    int32_t kind;      // lbm_bc_kind
+};
+
+// Per-list boundary parameters (device table).
+struct ListParam {
+    double rho;        // outlet density
+    double dir[3];     // inlet direction
+    int64_t amp_off;   // offset into the amplitude table array
+    int64_t amp_len;   // period of the amplitude table (>= 1)
+    int32_t kind;
+    int32_t pad;
+};
+
+// Per-instance parameters.
+struct InstParam {
+    double omega;      // 1/tau
+    float omega_f;
+    float pad;
+};
+
+// Storage formats.  Shifted formats hold (f - w) scaled; FP64/FP32 hold f.
+enum Store { ST_F64 = 0, ST_F32 = 1, ST_F16S = 2, ST_BF16S = 3 };
+constexpr float kF16Scale = 32768.0f;    // 2^15 keeps small deviations out of FP16 subnormals
+
+template <int S> struct StoreT;
+template <> struct StoreT<ST_F64> { using T = double; static constexpr int bytes = 8; };
+template <> struct StoreT<ST_F32> { using T = float; static constexpr int bytes = 4; };
+template <> struct StoreT<ST_F16S> { using T = __half; static constexpr int bytes = 2; };
+template <> struct StoreT<ST_BF16S> { using T = __nv_bfloat16; static constexpr int bytes = 2; };
+
+// Arguments of one step launch.
+struct StepArgs {
+    const Chunk* chunks;
+    int64_t nchunks;
+    const void* src;          // populations read (pull) / the single lattice (AA)
+    void* dst;                // populations written (pull) / same as src (AA)
+    int64_t stride;           // elements between population planes (SoA)
+    const ZSlot* zslots;
+    const ListParam* lists;
+    const InstParam* insts;
+    const double* amp;        // concatenated amplitude tables
+    int64_t step;             // reference iteration index of this step
+    const int64_t* step_base; // when non-null, added to step (graph replays)
+    // snapshot outputs (dry launch only): f (node-major, Q per node), rho, u (3 per node)
+    double* out_f;
+    double* out_rho;
+    double* out_u;
+    int64_t n_nodes;
+};
+
+}  // namespace lbm
+
+// CUDA error check for host code returning lbm_status.
+#define LBM_CUDA(call)                                                                          \
+    do {                                                                                        \
+        cudaError_t e_ = (call);                                                                \
+        if (e_ != cudaSuccess)                                                                  \
+            return ::lbm::fail(LBM_ERR_CUDA, "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), \
+                               __FILE__, __LINE__);                                             \
+    } while (0)

@@ -1,0 +1,27 @@
+// Internal declarations shared by the host-side translation units of
+// liblbm_gb300.so (not installed, not part of the ABI).
+#pragma once
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "lbm_gb300.h"
+
+namespace lbm {
+
+// Records the message for lbm_last_error() and returns the status.
+lbm_status fail(lbm_status s, const char* fmt, ...);
+void clear_error();
+
+// Triangle array helpers (host).
+using TriVec = std::vector<lbm_tri>;
+lbm_status to_c_array(const TriVec& v, lbm_tri** out, size_t* n);
+
+// Marching-tetrahedra mesher over an implicit function given at grid vertices.
+struct CapsuleSet;
+lbm_status mesh_capsules(const double* seg, size_t nseg, const double lo[3], const double hi[3], double h,
+                         uint64_t seed, TriVec& out);
+
+}  // namespace lbm

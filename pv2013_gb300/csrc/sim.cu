@@ -1,0 +1,751 @@
+// Device lattice construction and the simulation handle (host orchestration +
+// set-up kernels).  Replaces SubDomain (Subdomain.cpp:3-33, :375-651) and the
+// Simulation driver (Simulation.cpp:3-13, :903-932) for one GPU.
+//
+// Lattice layout in HBM
+//   populations   SoA planes, plane q holds population q of every node
+//                 (node id = x-major order of the fluid points, z fastest);
+//                 plane stride padded to 64 elements (128 B for 16-bit types);
+//                 two planes sets for the pull pattern, one for AA
+//   chunks        one 128-byte descriptor per <=32-node z-run piece (see
+//                 device.cuh): the only per-step index traffic, ~4-6 B/node
+//   Zou-He slots  16 B per inlet/outlet node; list and instance tables
+// Node typing follows CreateNodes (Subdomain.cpp:399-477): a boundary point
+// takes the first predicate list that contains it (lowest list id, the
+// reference's Inlet, Outlet1..6 order); boundary points in no list are wall
+// nodes; other fluid points are interior nodes.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "device.cuh"
+#include "internal.h"
+#include "scan.cuh"
+#include "step.h"
+#include "step_kernel.cuh"
+
+namespace lbm {
+// geometry accessors (geometry.cu)
+const uint8_t* geometry_flags_dev(const lbm_geometry* g);
+const int64_t* geometry_bidx_dev(const lbm_geometry* g);
+const uint64_t* geometry_bmask_dev(const lbm_geometry* g);
+int64_t geometry_nboundary(const lbm_geometry* g);
+int64_t geometry_nfluid(const lbm_geometry* g);
+void geometry_dims(const lbm_geometry* g, int dims[3]);
+int geometry_device(const lbm_geometry* g);
+}  // namespace lbm
+
+using namespace lbm;
+
+extern "C" void lbm_sim_destroy(lbm_sim* S);
+
+#define LBM_TRY(x)                      \
+    do {                                \
+        lbm_status s_ = (x);            \
+        if (s_ != LBM_OK) return s_;    \
+    } while (0)
+
+namespace {
+
+template <class T>
+struct DBuf {
+    T* p = nullptr;
+    DBuf() = default;
+    DBuf(const DBuf&) = delete;
+    ~DBuf() { if (p) cudaFree(p); }
+    lbm_status alloc(size_t n, const char* what) {
+        if (p) { cudaFree(p); p = nullptr; }
+        if (cudaMalloc(&p, sizeof(T) * (n ? n : 1)) != cudaSuccess)
+            return fail(LBM_ERR_NOMEM, "cudaMalloc for %s (%zu elements) failed", what, n);
+        return LBM_OK;
+    }
+    T* release() { T* q = p; p = nullptr; return q; }
+};
+
+int blocks_for(int64_t n, int threads) {
+    int64_t b = (n + threads - 1) / threads;
+    if (b > 152LL * 64) b = 152LL * 64;
+    return (int)std::max<int64_t>(b, 1);
+}
+
+// --------------------------------------------------------------------------
+// set-up kernels
+
+__global__ void k_scatter_ids(const int64_t* __restrict__ node_grid, int64_t n, int32_t* __restrict__ node_of_point) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        node_of_point[node_grid[i]] = (int32_t)i;
+}
+
+// role: 0 interior, 1 wall, 2+l first matching predicate list l
+__global__ void k_roles(const int64_t* __restrict__ bidx, const uint64_t* __restrict__ bmask, int64_t nb,
+                        const int32_t* __restrict__ node_of_point, int8_t* __restrict__ role) {
+    for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < nb; b += (int64_t)gridDim.x * blockDim.x) {
+        const int32_t n = node_of_point[bidx[b]];
+        const uint64_t m = bmask[b];
+        role[n] = m ? (int8_t)(2 + __ffsll((long long)m) - 1) : (int8_t)1;
+    }
+}
+
+__global__ void k_zflag(const int8_t* __restrict__ role, int64_t n, uint64_t zlists, uint8_t* __restrict__ z) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int r = role[i];
+        z[i] = (r >= 2 && ((zlists >> (r - 2)) & 1ull)) ? 1 : 0;
+    }
+}
+
+__global__ void k_gather_role(const int64_t* __restrict__ ids, int64_t n, const int8_t* __restrict__ role,
+                              int8_t* __restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        out[i] = role[ids[i]];
+}
+
+// chunks per grid column
+__global__ void k_col_count(const uint8_t* __restrict__ flags, int Nx, int Ny, int Nz, int32_t* __restrict__ cnt) {
+    const int64_t ncol = (int64_t)Nx * Ny;
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncol; c += (int64_t)gridDim.x * blockDim.x) {
+        const uint8_t* f = flags + c * Nz;
+        int32_t n = 0;
+        int run = 0;
+        for (int k = 0; k <= Nz; ++k) {
+            const bool fl = k < Nz && f[k];
+            if (fl) ++run;
+            if (!fl || run == 32) {
+                if (run > 0) ++n;
+                run = 0;
+            }
+        }
+        cnt[c] = n;
+    }
+}
+
+struct FillArgs {
+    const uint8_t* flags;
+    int Nx, Ny, Nz;
+    const int64_t* chunk_off;     // per column
+    const int32_t* node_of_point; // local ids
+    const int8_t* role;
+    const int64_t* znodes;        // sorted local ids of Zou-He nodes
+    int64_t nz;
+    int64_t node_off, zslot_off;
+    int32_t inst;
+    Chunk* chunks;
+};
+
+__device__ int64_t lower_bound_i64(const int64_t* a, int64_t n, int64_t v) {
+    int64_t lo = 0, hi = n;
+    while (lo < hi) {
+        int64_t mid = (lo + hi) >> 1;
+        if (a[mid] < v) lo = mid + 1; else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void k_col_fill(FillArgs A) {
+    const int64_t ncol = (int64_t)A.Nx * A.Ny;
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncol; c += (int64_t)gridDim.x * blockDim.x) {
+        const int i = (int)(c / A.Ny), j = (int)(c % A.Ny);
+        const uint8_t* f = A.flags + c * A.Nz;
+        int64_t out = A.chunk_off[c];
+        int run = 0, k0 = 0;
+        for (int k = 0; k <= A.Nz; ++k) {
+            const bool fl = k < A.Nz && f[k];
+            if (fl) { if (run == 0) k0 = k; ++run; }
+            if (!fl || run == 32) {
+                if (run > 0) {
+                    Chunk ch;
+                    const int32_t n0 = A.node_of_point[c * A.Nz + k0];
+                    ch.n0 = (int32_t)(A.node_off + n0);
+                    ch.len_inst = (uint32_t)run | ((uint32_t)A.inst << 8);
+                    ch.wmask = 0;
+                    ch.zmask = 0;
+                    for (int t = 0; t < run; ++t) {
+                        const int r = A.role[n0 + t];
+                        if (r == 1) ch.wmask |= 1u << t;
+                    }
+                    const int64_t zfirst = lower_bound_i64(A.znodes, A.nz, n0);
+                    ch.zslot0 = (int32_t)(A.zslot_off + zfirst);
+                    for (int64_t zz = zfirst; zz < A.nz && A.znodes[zz] < n0 + run; ++zz)
+                        ch.zmask |= 1u << (int)(A.znodes[zz] - n0);
+                    for (int di = -1; di <= 1; ++di)
+                        for (int dj = -1; dj <= 1; ++dj) {
+                            const int d = (di + 1) * 3 + (dj + 1);
+                            const int a = i + di, b = j + dj;
+                            uint64_t m = 0;
+                            int32_t base = 0;
+                            if (a >= 0 && a < A.Nx && b >= 0 && b < A.Ny) {
+                                const int64_t cc = (int64_t)a * A.Ny + b;
+                                const uint8_t* g = A.flags + cc * A.Nz;
+                                int first = -1;
+                                for (int bit = 0; bit < 34; ++bit) {
+                                    const int kk = k0 - 1 + bit;
+                                    if (kk >= 0 && kk < A.Nz && g[kk]) {
+                                        m |= 1ull << bit;
+                                        if (first < 0) first = kk;
+                                    }
+                                }
+                                if (first >= 0) base = (int32_t)(A.node_off + A.node_of_point[cc * A.Nz + first]);
+                            }
+                            ch.mask[d] = m;
+                            ch.base[d] = base;
+                        }
+                    A.chunks[out++] = ch;
+                }
+                run = 0;
+            }
+        }
+    }
+}
+
+template <class T>
+__global__ void k_init_pop(T* __restrict__ a, int64_t stride, int Q, const double* __restrict__ val) {
+    const int64_t n = stride * Q;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int q = (int)(i / stride);
+        a[i] = (T)val[q];
+    }
+}
+__global__ void k_init_half(__half* a, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        a[i] = __float2half_rn(0.0f);
+}
+__global__ void k_init_bf16(__nv_bfloat16* a, int64_t n) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        a[i] = __float2bfloat16_rn(0.0f);
+}
+
+__global__ void k_add_step(int64_t* base, int64_t inc) { *base += inc; }
+
+struct MonOut {
+    double mass, inflow, outflow, maxu;
+    int32_t bad;
+};
+
+__global__ void k_reduce_partials(Partials p, int64_t nblocks, MonOut* out) {
+    // fixed-order reduction: thread t sums a contiguous range, then a
+    // fixed tree over 256 threads (deterministic for a given block count)
+    __shared__ double s[4][256];
+    __shared__ int sb[256];
+    const int t = threadIdx.x;
+    const int64_t per = (nblocks + 255) / 256;
+    const int64_t b = t * per, e = min(nblocks, b + per);
+    double a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+    int bb = 0;
+    for (int64_t i = b; i < e; ++i) {
+        a0 += p.mass[i]; a1 += p.inflow[i]; a2 += p.outflow[i]; a3 = fmax(a3, p.maxu[i]); bb |= p.bad[i];
+    }
+    s[0][t] = a0; s[1][t] = a1; s[2][t] = a2; s[3][t] = a3; sb[t] = bb;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (t < o) {
+            s[0][t] += s[0][t + o]; s[1][t] += s[1][t + o]; s[2][t] += s[2][t + o];
+            s[3][t] = fmax(s[3][t], s[3][t + o]); sb[t] |= sb[t + o];
+        }
+        __syncthreads();
+    }
+    if (t == 0) { out->mass = s[0][0]; out->inflow = s[1][0]; out->outflow = s[2][0]; out->maxu = s[3][0]; out->bad = sb[0]; }
+}
+
+int store_of(int precision) {
+    switch (precision) {
+        case LBM_F64: return ST_F64;
+        case LBM_F32: return ST_F32;
+        case LBM_F16S: return ST_F16S;
+        case LBM_BF16S: return ST_BF16S;
+    }
+    return -1;
+}
+int store_bytes(int s) { return s == ST_F64 ? 8 : (s == ST_F32 ? 4 : 2); }
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+
+struct lbm_sim {
+    int dev = 0;
+    int Q = 19, store = ST_F64, pattern = LBM_PULL, wpb = 4;
+    int64_t N = 0, nchunks = 0, stride = 0, nz = 0;
+    int64_t n_inst = 0;
+    void* buf[2] = {nullptr, nullptr};
+    int cur = 0;                   // pull: buffer holding the current state
+    Chunk* chunks = nullptr;
+    ZSlot* zslots = nullptr;
+    ListParam* lists = nullptr;
+    InstParam* insts = nullptr;
+    double* amp = nullptr;
+    int64_t* node_grid = nullptr;  // grid index per node (per instance)
+    std::vector<int64_t> inst_off; // node offsets, n_inst + 1
+    int64_t steps_done = 0;
+    // graph replay
+    cudaGraphExec_t gexec = nullptr;
+    cudaGraph_t graph = nullptr;
+    int64_t glen = 0;
+    int gcur = 0;
+    int64_t* step_base = nullptr;
+    // monitors
+    double* part = nullptr;        // 4 * nblocks doubles
+    int32_t* partbad = nullptr;
+    MonOut* mon = nullptr;
+    int64_t part_blocks = 0;
+    double mass0 = 0.0;
+    double div_tol = 1e-2;
+};
+
+namespace {
+
+struct InstBuild {
+    int64_t N = 0;
+    DBuf<int64_t> node_grid;
+    DBuf<Chunk> chunks;
+    int64_t nchunks = 0;
+    std::vector<ZSlot> zslots;
+};
+
+lbm_status build_instance(const lbm_geometry* g, const lbm_sim_params* p, int32_t inst, int64_t node_off,
+                          int64_t zslot_off, cudaStream_t st, InstBuild& out) {
+    int dims[3];
+    geometry_dims(g, dims);
+    const int64_t npts = (int64_t)dims[0] * dims[1] * dims[2];
+    const uint8_t* flags = geometry_flags_dev(g);
+    // 1. node numbering (x-major compaction of Fluid points)
+    int64_t* ng = nullptr;
+    LBM_TRY(scan::compact(flags, npts, &ng, &out.N, st));
+    out.node_grid.p = ng;
+    if (out.N == 0) return fail(LBM_ERR_ARG, "instance %d has no fluid node", inst);
+    if (node_off + out.N >= INT32_MAX) return fail(LBM_ERR_ARG, "more than 2^31 nodes");
+    DBuf<int32_t> nop;
+    LBM_TRY(nop.alloc(npts, "node map"));
+    LBM_CUDA(cudaMemsetAsync(nop.p, 0xff, sizeof(int32_t) * npts, st));
+    k_scatter_ids<<<blocks_for(out.N, 256), 256, 0, st>>>(ng, out.N, nop.p);
+    // 2. roles
+    DBuf<int8_t> role;
+    LBM_TRY(role.alloc(out.N, "node roles"));
+    LBM_CUDA(cudaMemsetAsync(role.p, 0, out.N, st));
+    const int64_t nb = geometry_nboundary(g);
+    if (nb) k_roles<<<blocks_for(nb, 256), 256, 0, st>>>(geometry_bidx_dev(g), geometry_bmask_dev(g), nb, nop.p, role.p);
+    // 3. Zou-He nodes: role list with a boundary-condition kind
+    int kind[64] = {0};
+    const lbm_list_bc* lbc[64] = {nullptr};
+    for (size_t b = 0; b < p->nbcs; ++b) {
+        const lbm_list_bc& L = p->bcs[b];
+        if (L.list_id < 0 || L.list_id > 63) return fail(LBM_ERR_ARG, "bc %zu: list id %d", b, L.list_id);
+        kind[L.list_id] = L.kind;
+        lbc[L.list_id] = &L;
+    }
+    uint64_t zl = 0;
+    for (int l = 0; l < 64; ++l) if (kind[l] != LBM_BC_NONE) zl |= 1ull << l;
+    DBuf<uint8_t> zf;
+    LBM_TRY(zf.alloc(out.N, "zou-he flags"));
+    k_zflag<<<blocks_for(out.N, 256), 256, 0, st>>>(role.p, out.N, zl, zf.p);
+    int64_t* zn = nullptr;
+    int64_t nzn = 0;
+    LBM_TRY(scan::compact(zf.p, out.N, &zn, &nzn, st));
+    DBuf<int64_t> znodes; znodes.p = zn;
+    {
+        DBuf<int8_t> zr;
+        LBM_TRY(zr.alloc(nzn, "zou-he roles"));
+        if (nzn) k_gather_role<<<blocks_for(nzn, 256), 256, 0, st>>>(zn, nzn, role.p, zr.p);
+        std::vector<int8_t> hr(nzn);
+        if (nzn) LBM_CUDA(cudaMemcpyAsync(hr.data(), zr.p, nzn, cudaMemcpyDeviceToHost, st));
+        LBM_CUDA(cudaStreamSynchronize(st));
+        std::vector<int64_t> rank(64, 0);
+        out.zslots.resize(nzn);
+        for (int64_t s = 0; s < nzn; ++s) {
+            const int l = hr[s] - 2;
+            const lbm_list_bc* L = lbc[l];
+            ZSlot z;
+            z.list = inst * 64 + l;
+            z.kind = kind[l];
+            const int64_t r = rank[l]++;
+            z.profile = 1.0;
+            if (L && L->profile) {
+                if ((size_t)r >= L->profile_len)
+                    return fail(LBM_ERR_ARG, "list %d: profile has %zu entries, fewer than the list's nodes", l,
+                                L->profile_len);
+                z.profile = L->profile[r];
+            }
+            out.zslots[s] = z;
+        }
+        for (int l = 0; l < 64; ++l) {
+            const lbm_list_bc* L = lbc[l];
+            if (L && L->profile && L->profile_len != (size_t)rank[l])
+                return fail(LBM_ERR_ARG, "list %d: profile has %zu entries, list has %lld nodes", l, L->profile_len,
+                            (long long)rank[l]);
+        }
+    }
+    // 4. chunks
+    const int64_t ncol = (int64_t)dims[0] * dims[1];
+    DBuf<int32_t> ccount;
+    DBuf<int64_t> coff;
+    LBM_TRY(ccount.alloc(ncol, "chunk counts"));
+    LBM_TRY(coff.alloc(ncol, "chunk offsets"));
+    k_col_count<<<blocks_for(ncol, 128), 128, 0, st>>>(flags, dims[0], dims[1], dims[2], ccount.p);
+    LBM_TRY(scan::exclusive_scan(ccount.p, ncol, coff.p, &out.nchunks, st));
+    LBM_TRY(out.chunks.alloc(out.nchunks, "chunks"));
+    FillArgs fa;
+    fa.flags = flags; fa.Nx = dims[0]; fa.Ny = dims[1]; fa.Nz = dims[2];
+    fa.chunk_off = coff.p; fa.node_of_point = nop.p; fa.role = role.p;
+    fa.znodes = zn; fa.nz = nzn; fa.node_off = node_off; fa.zslot_off = zslot_off; fa.inst = inst;
+    fa.chunks = out.chunks.p;
+    k_col_fill<<<blocks_for(ncol, 128), 128, 0, st>>>(fa);
+    LBM_CUDA(cudaGetLastError());
+    LBM_CUDA(cudaStreamSynchronize(st));
+    return LBM_OK;
+}
+
+lbm_status sim_launch(lbm_sim* S, int mode, bool dry, void* src, void* dst, int64_t step, const int64_t* step_base,
+                      const Partials& part, double* of, double* orho, double* ou, cudaStream_t st) {
+    StepArgs a;
+    a.chunks = S->chunks; a.nchunks = S->nchunks;
+    a.src = src; a.dst = dst; a.stride = S->stride;
+    a.zslots = S->zslots; a.lists = S->lists; a.insts = S->insts; a.amp = S->amp;
+    a.step = step; a.step_base = step_base;
+    a.out_f = of; a.out_rho = orho; a.out_u = ou; a.n_nodes = S->N;
+    if (S->store == ST_F64) return launch_step_f64(S->Q, mode, dry, a, part, S->wpb, st);
+    return launch_step_lp(S->Q, S->store, mode, dry, a, part, S->wpb, st);
+}
+
+// Launches one step at the current state; advances cur/steps_done.
+lbm_status sim_one_step(lbm_sim* S, int64_t step_arg, const int64_t* step_base, cudaStream_t st, bool advance_count) {
+    Partials np = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    lbm_status s;
+    if (S->pattern == LBM_PULL) {
+        s = sim_launch(S, MODE_PULL, false, S->buf[S->cur], S->buf[1 - S->cur], step_arg, step_base, np, nullptr,
+                       nullptr, nullptr, st);
+        S->cur = 1 - S->cur;
+    } else {
+        const int mode = ((S->steps_done & 1) == 0) ? MODE_AA_EVEN : MODE_AA_ODD;
+        s = sim_launch(S, mode, false, S->buf[0], S->buf[0], step_arg, step_base, np, nullptr, nullptr, nullptr, st);
+    }
+    if (advance_count) S->steps_done++;
+    return s;
+}
+
+// Dry launch at the current state (fields and/or monitor partials).
+lbm_status sim_dry(lbm_sim* S, double* of, double* orho, double* ou, bool partials, cudaStream_t st) {
+    Partials p = {nullptr, nullptr, nullptr, nullptr, nullptr};
+    if (partials) {
+        p.mass = S->part;
+        p.inflow = S->part + S->part_blocks;
+        p.outflow = S->part + 2 * S->part_blocks;
+        p.maxu = S->part + 3 * S->part_blocks;
+        p.bad = S->partbad;
+    }
+    int mode;
+    void* src;
+    if (S->pattern == LBM_PULL) { mode = MODE_PULL; src = S->buf[S->cur]; }
+    else { mode = ((S->steps_done & 1) == 0) ? MODE_AA_EVEN : MODE_AA_ODD; src = S->buf[0]; }
+    LBM_TRY(sim_launch(S, mode, true, src, src, S->steps_done, nullptr, p, of, orho, ou, st));
+    if (partials) k_reduce_partials<<<1, 256, 0, st>>>(p, S->part_blocks, S->mon);
+    LBM_CUDA(cudaGetLastError());
+    return LBM_OK;
+}
+
+lbm_status sim_monitors(lbm_sim* S, lbm_monitors* out, cudaStream_t st) {
+    LBM_TRY(sim_dry(S, nullptr, nullptr, nullptr, true, st));
+    MonOut h;
+    LBM_CUDA(cudaMemcpyAsync(&h, S->mon, sizeof h, cudaMemcpyDeviceToHost, st));
+    LBM_CUDA(cudaStreamSynchronize(st));
+    out->step = S->steps_done;
+    out->mass = h.mass;
+    out->inlet_flux = h.inflow;
+    out->outlet_flux = h.outflow;
+    out->max_speed = h.maxu;
+    out->nonfinite = h.bad;
+    return LBM_OK;
+}
+
+void free_graph(lbm_sim* S) {
+    if (S->gexec) cudaGraphExecDestroy(S->gexec);
+    if (S->graph) cudaGraphDestroy(S->graph);
+    S->gexec = nullptr;
+    S->graph = nullptr;
+    S->glen = 0;
+}
+
+lbm_status sim_create(const lbm_geometry* const* g, const lbm_sim_params* p, size_t n, cudaStream_t st, lbm_sim** out) {
+    std::unique_ptr<lbm_sim, void (*)(lbm_sim*)> S(new lbm_sim(), lbm_sim_destroy);
+    cudaGetDevice(&S->dev);
+    const lbm_sim_params& p0 = p[0];
+    if (p0.Q != 19 && p0.Q != 27) return fail(LBM_ERR_ARG, "Q must be 19 or 27 (got %d)", p0.Q);
+    S->Q = p0.Q;
+    S->store = store_of(p0.precision);
+    if (S->store < 0) return fail(LBM_ERR_ARG, "unknown precision %d", p0.precision);
+    S->pattern = p0.pattern == LBM_AUTO ? LBM_AA : p0.pattern;
+    if (S->pattern != LBM_PULL && S->pattern != LBM_AA) return fail(LBM_ERR_ARG, "unknown pattern %d", p0.pattern);
+    S->wpb = p0.warps_per_block > 0 ? p0.warps_per_block : 4;
+    if (S->wpb > 16) return fail(LBM_ERR_ARG, "warps_per_block must be <= 16");
+    for (size_t i = 0; i < n; ++i) {
+        if (p[i].Q != p0.Q || p[i].precision != p0.precision || p[i].pattern != p0.pattern)
+            return fail(LBM_ERR_ARG, "batch members must share Q, precision and pattern");
+        if (!(p[i].tau > 0.5)) return fail(LBM_ERR_ARG, "instance %zu: tau must be > 0.5 (got %g)", i, p[i].tau);
+        if (geometry_device(g[i]) != S->dev) return fail(LBM_ERR_ARG, "geometry %zu lives on another device", i);
+    }
+    S->n_inst = (int64_t)n;
+    std::vector<std::unique_ptr<InstBuild>> builds;
+    std::vector<ZSlot> zall;
+    int64_t node_off = 0, nch = 0;
+    S->inst_off.push_back(0);
+    for (size_t i = 0; i < n; ++i) {
+        builds.emplace_back(new InstBuild());
+        LBM_TRY(build_instance(g[i], &p[i], (int32_t)i, node_off, (int64_t)zall.size(), st, *builds.back()));
+        node_off += builds.back()->N;
+        nch += builds.back()->nchunks;
+        zall.insert(zall.end(), builds.back()->zslots.begin(), builds.back()->zslots.end());
+        S->inst_off.push_back(node_off);
+    }
+    S->N = node_off;
+    S->nchunks = nch;
+    S->nz = (int64_t)zall.size();
+    // concatenate per-instance arrays
+    LBM_CUDA(cudaMalloc(&S->chunks, sizeof(Chunk) * std::max<int64_t>(nch, 1)));
+    LBM_CUDA(cudaMalloc(&S->node_grid, sizeof(int64_t) * S->N));
+    int64_t co = 0;
+    for (size_t i = 0; i < n; ++i) {
+        LBM_CUDA(cudaMemcpyAsync(S->chunks + co, builds[i]->chunks.p, sizeof(Chunk) * builds[i]->nchunks,
+                                 cudaMemcpyDeviceToDevice, st));
+        LBM_CUDA(cudaMemcpyAsync(S->node_grid + S->inst_off[i], builds[i]->node_grid.p, sizeof(int64_t) * builds[i]->N,
+                                 cudaMemcpyDeviceToDevice, st));
+        co += builds[i]->nchunks;
+    }
+    LBM_CUDA(cudaMalloc(&S->zslots, sizeof(ZSlot) * std::max<size_t>(zall.size(), 1)));
+    if (!zall.empty())
+        LBM_CUDA(cudaMemcpyAsync(S->zslots, zall.data(), sizeof(ZSlot) * zall.size(), cudaMemcpyHostToDevice, st));
+    // list, amplitude and instance tables
+    std::vector<ListParam> lists(64 * n);
+    std::vector<double> amp;
+    std::vector<InstParam> insts(n);
+    for (size_t i = 0; i < n; ++i) {
+        insts[i].omega = 1.0 / p[i].tau;
+        insts[i].omega_f = (float)insts[i].omega;
+        insts[i].pad = 0.f;
+        for (int l = 0; l < 64; ++l) {
+            ListParam& L = lists[64 * i + l];
+            std::memset(&L, 0, sizeof L);
+            L.rho = 1.0;
+            L.amp_off = 0;
+            L.amp_len = 1;
+        }
+        for (size_t b = 0; b < p[i].nbcs; ++b) {
+            const lbm_list_bc& B = p[i].bcs[b];
+            ListParam& L = lists[64 * i + B.list_id];
+            L.kind = B.kind;
+            L.rho = B.rho;
+            for (int a = 0; a < 3; ++a) L.dir[a] = B.dir[a];
+            L.amp_off = (int64_t)amp.size() + 1;   // entry 0 of the table is the constant 1
+            if (B.amp && B.amp_len) {
+                L.amp_len = (int64_t)B.amp_len;
+                amp.insert(amp.end(), B.amp, B.amp + B.amp_len);
+            } else {
+                L.amp_len = 1;
+                amp.push_back(1.0);
+            }
+            if (p0.Q == 19 && B.kind == LBM_BC_VEL_POSX) return fail(LBM_ERR_ARG, "LBM_BC_VEL_POSX needs Q=27");
+            if (p0.Q == 27 && B.kind != LBM_BC_VEL_POSX && B.kind != LBM_BC_NONE)
+                return fail(LBM_ERR_ARG, "Q=27 supports the reference's D3Q27 inlet (LBM_BC_VEL_POSX) only");
+        }
+    }
+    amp.insert(amp.begin(), 1.0);
+    LBM_CUDA(cudaMalloc(&S->lists, sizeof(ListParam) * lists.size()));
+    LBM_CUDA(cudaMemcpyAsync(S->lists, lists.data(), sizeof(ListParam) * lists.size(), cudaMemcpyHostToDevice, st));
+    LBM_CUDA(cudaMalloc(&S->amp, sizeof(double) * amp.size()));
+    LBM_CUDA(cudaMemcpyAsync(S->amp, amp.data(), sizeof(double) * amp.size(), cudaMemcpyHostToDevice, st));
+    LBM_CUDA(cudaMalloc(&S->insts, sizeof(InstParam) * n));
+    LBM_CUDA(cudaMemcpyAsync(S->insts, insts.data(), sizeof(InstParam) * n, cudaMemcpyHostToDevice, st));
+    // populations, initial f = w (Node.cpp:30-37): stored w for F64/F32, 0 for shifted
+    S->stride = (S->N + 63) / 64 * 64;
+    const int nb = S->pattern == LBM_PULL ? 2 : 1;
+    const size_t bytes = (size_t)S->stride * S->Q * store_bytes(S->store);
+    std::vector<double> wv(S->Q);
+    for (int q = 0; q < S->Q; ++q) wv[q] = S->Q == 19 ? Lat<19>::w(q) : Lat<27>::w(q);
+    DBuf<double> dw;
+    LBM_TRY(dw.alloc(S->Q, "weights"));
+    LBM_CUDA(cudaMemcpyAsync(dw.p, wv.data(), sizeof(double) * S->Q, cudaMemcpyHostToDevice, st));
+    for (int b = 0; b < nb; ++b) {
+        if (cudaMalloc(&S->buf[b], bytes) != cudaSuccess)
+            return fail(LBM_ERR_NOMEM, "cudaMalloc of %zu bytes of populations failed", bytes);
+        const int64_t tot = S->stride * S->Q;
+        if (S->store == ST_F64) k_init_pop<double><<<blocks_for(tot, 256), 256, 0, st>>>((double*)S->buf[b], S->stride, S->Q, dw.p);
+        else if (S->store == ST_F32) k_init_pop<float><<<blocks_for(tot, 256), 256, 0, st>>>((float*)S->buf[b], S->stride, S->Q, dw.p);
+        else if (S->store == ST_F16S) k_init_half<<<blocks_for(tot, 256), 256, 0, st>>>((__half*)S->buf[b], tot);
+        else k_init_bf16<<<blocks_for(tot, 256), 256, 0, st>>>((__nv_bfloat16*)S->buf[b], tot);
+    }
+    // monitor buffers (one partial per block of the dry launch)
+    S->part_blocks = std::max<int64_t>((S->nchunks + S->wpb - 1) / S->wpb, 1);
+    LBM_CUDA(cudaMalloc(&S->part, sizeof(double) * 4 * S->part_blocks));
+    LBM_CUDA(cudaMalloc(&S->partbad, sizeof(int32_t) * S->part_blocks));
+    LBM_CUDA(cudaMalloc(&S->mon, sizeof(MonOut)));
+    LBM_CUDA(cudaMalloc(&S->step_base, sizeof(int64_t)));
+    LBM_CUDA(cudaGetLastError());
+    LBM_CUDA(cudaStreamSynchronize(st));
+    lbm_monitors m;
+    LBM_TRY(sim_monitors(S.get(), &m, st));
+    S->mass0 = m.mass;
+    *out = S.release();
+    return LBM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+lbm_status lbm_sim_create(const lbm_geometry* g, const lbm_sim_params* p, void* stream, lbm_sim** out) {
+    if (!g || !p || !out) return fail(LBM_ERR_ARG, "lbm_sim_create: null argument");
+    clear_error();
+    *out = nullptr;
+    lbm_sim* S = nullptr;
+    lbm_status s = sim_create(&g, p, 1, (cudaStream_t)stream, &S);
+    if (s != LBM_OK) return s;
+    *out = S;
+    return LBM_OK;
+}
+
+lbm_status lbm_batch_create(const lbm_geometry* const* g, const lbm_sim_params* p, size_t n, void* stream,
+                            lbm_sim** out) {
+    if (!g || !p || !out || n == 0) return fail(LBM_ERR_ARG, "lbm_batch_create: bad argument");
+    if (n >= (1u << 24)) return fail(LBM_ERR_ARG, "lbm_batch_create: too many instances");
+    clear_error();
+    *out = nullptr;
+    lbm_sim* S = nullptr;
+    lbm_status s = sim_create(g, p, n, (cudaStream_t)stream, &S);
+    if (s != LBM_OK) return s;
+    *out = S;
+    return LBM_OK;
+}
+
+lbm_status lbm_sim_step(lbm_sim* S, int64_t nsteps, uint32_t flags, void* stream) {
+    if (!S || nsteps < 0) return fail(LBM_ERR_ARG, "lbm_sim_step: bad argument");
+    clear_error();
+    cudaStream_t st = (cudaStream_t)stream;
+    int64_t left = nsteps;
+    if ((flags & LBM_STEP_GRAPH) && nsteps >= 4) {
+        // state parity must match the captured graph: pull buffer index and
+        // AA step parity both return to their start after an even step count
+        if ((S->steps_done & 1) || (S->pattern == LBM_PULL && S->cur != 0)) {
+            LBM_TRY(sim_one_step(S, S->steps_done, nullptr, st, true));
+            --left;
+        }
+        const int64_t G = std::min<int64_t>(64, left & ~1LL);
+        if (G >= 2) {
+            if (S->glen != G) {
+                free_graph(S);
+                cudaStream_t cs;
+                LBM_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+                LBM_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+                const int cur0 = S->cur;
+                const int64_t sd0 = S->steps_done;
+                lbm_status ls = LBM_OK;
+                for (int64_t s = 0; s < G && ls == LBM_OK; ++s) {
+                    ls = sim_one_step(S, s, S->step_base, cs, false);
+                    S->steps_done++;   // parity for AA within the capture
+                }
+                k_add_step<<<1, 1, 0, cs>>>(S->step_base, G);
+                cudaError_t e = cudaStreamEndCapture(cs, &S->graph);
+                S->cur = cur0;
+                S->steps_done = sd0;
+                cudaStreamDestroy(cs);
+                if (ls != LBM_OK) return ls;
+                if (e != cudaSuccess) return fail(LBM_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+                LBM_CUDA(cudaGraphInstantiate(&S->gexec, S->graph, 0));
+                S->glen = G;
+            }
+            int64_t sd = S->steps_done;
+            LBM_CUDA(cudaMemcpyAsync(S->step_base, &sd, sizeof sd, cudaMemcpyHostToDevice, st));
+            while (left >= G) {
+                LBM_CUDA(cudaGraphLaunch(S->gexec, st));
+                S->steps_done += G;
+                left -= G;
+            }
+        }
+    }
+    for (; left > 0; --left) LBM_TRY(sim_one_step(S, S->steps_done, nullptr, st, true));
+    LBM_CUDA(cudaGetLastError());
+    if (flags & LBM_STEP_MONITOR) {
+        lbm_monitors m;
+        LBM_TRY(sim_monitors(S, &m, st));
+        if (m.nonfinite || !(std::fabs(m.mass / S->mass0 - 1.0) <= S->div_tol))
+            return fail(LBM_ERR_DIVERGED, "diverged at step %lld: mass %.17g (initial %.17g), non-finite=%d",
+                        (long long)S->steps_done, m.mass, S->mass0, m.nonfinite);
+    }
+    return LBM_OK;
+}
+
+lbm_status lbm_sim_info_get(const lbm_sim* S, lbm_sim_info* info) {
+    if (!S || !info) return fail(LBM_ERR_ARG, "lbm_sim_info_get: null argument");
+    std::memset(info, 0, sizeof *info);
+    info->n_nodes = S->N;
+    info->n_instances = S->n_inst;
+    info->steps_done = S->steps_done;
+    info->n_chunks = S->nchunks;
+    info->Q = S->Q;
+    info->precision = S->store;
+    info->pattern = S->pattern;
+    info->warps_per_block = S->wpb;
+    info->state_bytes = (int64_t)S->stride * S->Q * store_bytes(S->store) * (S->pattern == LBM_PULL ? 2 : 1);
+    info->algorithmic_bytes_per_update = 2.0 * S->Q * store_bytes(S->store);
+    return LBM_OK;
+}
+
+lbm_status lbm_sim_fields(lbm_sim* S, double* rho, double* u, double* f, size_t n_nodes, void* stream) {
+    if (!S) return fail(LBM_ERR_ARG, "lbm_sim_fields: null handle");
+    if (n_nodes < (size_t)S->N) return fail(LBM_ERR_ARG, "lbm_sim_fields: capacity %zu < %lld nodes", n_nodes, (long long)S->N);
+    clear_error();
+    cudaStream_t st = (cudaStream_t)stream;
+    DBuf<double> df, dr, du;
+    if (f) LBM_TRY(df.alloc((size_t)S->N * S->Q, "field f"));
+    if (rho) LBM_TRY(dr.alloc(S->N, "field rho"));
+    if (u) LBM_TRY(du.alloc((size_t)S->N * 3, "field u"));
+    LBM_TRY(sim_dry(S, df.p, dr.p, du.p, false, st));
+    if (f) LBM_CUDA(cudaMemcpyAsync(f, df.p, sizeof(double) * S->N * S->Q, cudaMemcpyDeviceToHost, st));
+    if (rho) LBM_CUDA(cudaMemcpyAsync(rho, dr.p, sizeof(double) * S->N, cudaMemcpyDeviceToHost, st));
+    if (u) LBM_CUDA(cudaMemcpyAsync(u, du.p, sizeof(double) * S->N * 3, cudaMemcpyDeviceToHost, st));
+    LBM_CUDA(cudaStreamSynchronize(st));
+    return LBM_OK;
+}
+
+lbm_status lbm_sim_nodes(const lbm_sim* S, int64_t* grid_index, size_t cap) {
+    if (!S || !grid_index) return fail(LBM_ERR_ARG, "lbm_sim_nodes: null argument");
+    if (cap < (size_t)S->N) return fail(LBM_ERR_ARG, "lbm_sim_nodes: capacity %zu < %lld", cap, (long long)S->N);
+    LBM_CUDA(cudaMemcpy(grid_index, S->node_grid, sizeof(int64_t) * S->N, cudaMemcpyDeviceToHost));
+    return LBM_OK;
+}
+
+lbm_status lbm_sim_instance_offsets(const lbm_sim* S, int64_t* off, size_t cap) {
+    if (!S || !off) return fail(LBM_ERR_ARG, "lbm_sim_instance_offsets: null argument");
+    if (cap < S->inst_off.size()) return fail(LBM_ERR_ARG, "lbm_sim_instance_offsets: capacity too small");
+    std::memcpy(off, S->inst_off.data(), sizeof(int64_t) * S->inst_off.size());
+    return LBM_OK;
+}
+
+lbm_status lbm_sim_monitors(lbm_sim* S, lbm_monitors* out, void* stream) {
+    if (!S || !out) return fail(LBM_ERR_ARG, "lbm_sim_monitors: null argument");
+    clear_error();
+    return sim_monitors(S, out, (cudaStream_t)stream);
+}
+
+lbm_status lbm_sim_set_divergence_tolerance(lbm_sim* S, double rel_tol) {
+    if (!S || !(rel_tol > 0)) return fail(LBM_ERR_ARG, "lbm_sim_set_divergence_tolerance: bad argument");
+    S->div_tol = rel_tol;
+    return LBM_OK;
+}
+
+void lbm_sim_destroy(lbm_sim* S) {
+    if (!S) return;
+    free_graph(S);
+    for (void* b : S->buf) if (b) cudaFree(b);
+    if (S->chunks) cudaFree(S->chunks);
+    if (S->zslots) cudaFree(S->zslots);
+    if (S->lists) cudaFree(S->lists);
+    if (S->insts) cudaFree(S->insts);
+    if (S->amp) cudaFree(S->amp);
+    if (S->node_grid) cudaFree(S->node_grid);
+    if (S->part) cudaFree(S->part);
+    if (S->partbad) cudaFree(S->partbad);
+    if (S->mon) cudaFree(S->mon);
+    if (S->step_base) cudaFree(S->step_base);
+    delete S;
+}
+
+}  // extern "C"

@@ -1,0 +1,401 @@
+// Fused lattice Boltzmann step: gather (streaming) + boundary conditions +
+// BGK collision + store, one warp per run-table chunk, one lane per node.
+//
+// One launch performs one Iterate() body of the reference
+// (Simulation.cpp:909-915) with the state kept in the populations array:
+//   gather      f_q(x) = f*_q(x - c_q)                     Streaming :184-198
+//   missing     source node absent (NotFluid or outside the grid):
+//                 wall node, q != the population the reference never bounces
+//                 back (opp of dir 0 for D3Q19)  -> f*_{opp q}(x)   ApplyWallBc :1353-1370
+//                 otherwise the population is never written by the reference
+//                 and keeps its initial value w_q (Node.cpp:30-37)
+//   Zou-He      velocity / pressure formulas on the node's own populations
+//                 (Boundary.cpp:87-148, Simulation.cpp:952-1348)
+//   collision   rho, u, f_eq, f* = omega f_eq + (1-omega) f  (Simulation.cpp:21-179)
+// The reference applies its boundary conditions after streaming and before
+// the next collision; here they run at the start of the next launch, which
+// is the same sequence of operations on every node.
+//
+// Streaming patterns:
+//   PULL     two lattices: read f*(step n-1) from src, write f*(step n) to dst
+//   AA_EVEN  one lattice, node-local: read slot q, write f*_q to slot opp(q)
+//   AA_ODD   one lattice, neighbour: read slot opp(q) of x - c_q, write f*_q
+//            to slot q of x + c_q (to slot opp(q) of x when x + c_q is absent)
+// DRY launches run the gather and boundary part only and write f_n, rho_n,
+// u_n in FP64 (snapshots and monitors); they never modify the state.
+//
+// Arithmetic: Store ST_F64 follows the reference's FP64 expressions operation
+// by operation (its TU is built with -fmad=false), so FP64 runs are bit-exact
+// with the reference.  The other stores compute in FP32 on shifted
+// populations f - w (rho - 1 and f_eq - w formed directly), which keeps the
+// small deviations representable.
+#pragma once
+#include "device.cuh"
+
+namespace lbm {
+
+enum StepMode { MODE_PULL = 0, MODE_AA_EVEN = 1, MODE_AA_ODD = 2 };
+
+template <int S> struct Work { using T = float; };
+template <> struct Work<ST_F64> { using T = double; };
+
+// storage -> working value (unshifted for F64, shifted otherwise)
+// (the read-only path is used for the pull pattern only: in the AA patterns
+// the kernel writes the array it reads)
+template <int S, int Q, bool RO = false>
+__device__ __forceinline__ typename Work<S>::T ld(const void* base, int64_t stride, int q, int64_t i) {
+    if constexpr (S == ST_F64) {
+        const double* p = (const double*)base + q * stride + i;
+        return RO ? __ldg(p) : *p;
+    } else if constexpr (S == ST_F32) {
+        const float* p = (const float*)base + q * stride + i;
+        return (RO ? __ldg(p) : *p) - (float)Lat<Q>::w(q);
+    } else if constexpr (S == ST_F16S) {
+        const __half h = ((const __half*)base)[q * stride + i];
+        return __half2float(h) * (1.0f / kF16Scale);
+    } else {
+        const __nv_bfloat16 h = ((const __nv_bfloat16*)base)[q * stride + i];
+        return __bfloat162float(h);
+    }
+}
+
+template <int S, int Q>
+__device__ __forceinline__ void st(void* base, int64_t stride, int q, int64_t i, typename Work<S>::T v) {
+    if constexpr (S == ST_F64) {
+        ((double*)base)[q * stride + i] = v;
+    } else if constexpr (S == ST_F32) {
+        ((float*)base)[q * stride + i] = v + (float)Lat<Q>::w(q);
+    } else if constexpr (S == ST_F16S) {
+        ((__half*)base)[q * stride + i] = __float2half_rn(v * kF16Scale);
+    } else {
+        ((__nv_bfloat16*)base)[q * stride + i] = __float2bfloat16_rn(v);
+    }
+}
+
+// plain (unshifted) value of a working value
+template <int S, int Q>
+__device__ __forceinline__ typename Work<S>::T plain(typename Work<S>::T v, int q) {
+    if constexpr (S == ST_F64) return v;
+    else return v + (float)Lat<Q>::w(q);
+}
+template <int S, int Q>
+__device__ __forceinline__ typename Work<S>::T unplain(typename Work<S>::T v, int q) {
+    if constexpr (S == ST_F64) return v;
+    else return v - (float)Lat<Q>::w(q);
+}
+
+// ---------------------------------------------------------------------------
+// Zou-He boundary formulas on plain populations, written in the reference's
+// operation order.  T = double reproduces the reference bit for bit.
+
+template <class T>
+__device__ __forceinline__ void zh_vel_negy(T* f, const T* v) {
+    // Boundary::ApplyBc, D3Q19 (Boundary.cpp:129-148)
+    T rhoN = (f[0] + f[1] + f[4] + f[5] + f[8] + f[9] + f[12] + f[13] + f[18] +
+              T(2.0) * (f[2] + f[6] + f[10] + f[14] + f[15])) / (T(1) + v[1]);
+    T Nx = T(0.5) * (f[0] + f[8] + f[9] - (f[1] + f[12] + f[13])) - (T(1.0) / T(3.0)) * rhoN * v[0];
+    T Nz = T(0.5) * (f[4] + f[8] + f[12] - (f[5] + f[9] + f[13])) - (T(1.0) / T(3.0)) * rhoN * v[2];
+    f[3] = f[2] - (T(1.0) / T(3.0)) * rhoN * v[1];
+    f[11] = f[6] + (T(1.0) / T(6.0)) * rhoN * (-v[1] - v[0]) + Nx;
+    f[7] = f[10] + (T(1.0) / T(6.0)) * rhoN * (-v[1] + v[0]) - Nx;
+    f[17] = f[14] + (T(1.0) / T(6.0)) * rhoN * (-v[1] - v[2]) + Nz;
+    f[16] = f[15] + (T(1.0) / T(6.0)) * rhoN * (-v[1] + v[2]) - Nz;
+}
+
+template <class T>
+__device__ __forceinline__ void zh_vel_posx_q27(T* f, const T* v) {
+    // Boundary::ApplyBc, D3Q27 (Boundary.cpp:87-123)
+    T rho = ((f[0] + f[3] + f[4] + f[5] + f[6] + f[15] + f[16] + f[17] + f[18]) +
+             T(2) * (f[2] + f[9] + f[10] + f[12] + f[14] + f[20] + f[22] + f[24] + f[26])) / (T(1) - v[0]);
+    T Ny = (T(1.0) / T(6)) * (f[3] + f[15] + f[16] - f[4] - f[17] - f[18]) - (T(1.0) / T(9)) * (rho * v[1]);
+    T Nz = (T(1.0) / T(6)) * (f[5] + f[15] + f[17] - f[6] - f[16] - f[18]) - (T(1.0) / T(9)) * (rho * v[2]);
+    f[1] = f[2] + (T(4) / T(9.0)) * rho * v[0];
+    f[7] = f[10] + (T(1) / T(9.0)) * rho * (v[0] + v[1]) - Ny;
+    f[8] = f[9] + (T(1) / T(9.0)) * rho * (v[0] - v[1]) + Ny;
+    f[11] = f[14] + (T(1) / T(9.0)) * rho * (v[0] + v[2]) - Nz;
+    f[13] = f[12] + (T(1) / T(9.0)) * rho * (v[0] - v[2]) + Nz;
+    f[19] = f[20] + (T(1) / T(36.0)) * rho * (v[0] + v[1] + v[2]) - Ny - Nz;
+    f[21] = f[22] + (T(1) / T(36.0)) * rho * (v[0] + v[1] - v[2]) - Ny + Nz;
+    f[23] = f[24] + (T(1) / T(36.0)) * rho * (v[0] - v[1] + v[2]) + Ny - Nz;
+    f[25] = f[26] + (T(1) / T(36.0)) * rho * (v[0] - v[1] - v[2]) + Ny + Nz;
+}
+
+// ApplyOutletBc bodies (Simulation.cpp:952-1348); transverse velocities are 0.
+template <class T>
+__device__ __forceinline__ void zh_press(T* f, int kind, T rho) {
+    const T vx = T(0.0), vz = T(0.0), vy0 = T(0.0);
+    if (kind == LBM_BC_PRESS_NEGY) {
+        T vy = T(-1) + (T(1.0) / rho) * (f[0] + f[1] + f[4] + f[5] + f[8] + f[9] + f[12] + f[13] + f[18] +
+                                         T(2.0) * (f[2] + f[6] + f[10] + f[14] + f[15]));
+        T Nyx = T(0.5) * (f[0] + f[8] + f[9] - (f[1] + f[12] + f[13])) - (T(1.0) / T(3.0)) * rho * vx;
+        T Nyz = T(0.5) * (f[4] + f[8] + f[12] - (f[5] + f[9] + f[13])) - (T(1.0) / T(3.0)) * rho * vz;
+        f[3] = f[2] - (T(1.0) / T(3.0)) * rho * vy;
+        f[11] = f[6] + (T(1.0) / T(6.0)) * rho * (-vx - vy) + Nyx;
+        f[7] = f[10] + (T(1.0) / T(6.0)) * rho * (vx - vy) - Nyx;
+        f[17] = f[14] + (T(1.0) / T(6.0)) * rho * (-vy - vz) + Nyz;
+        f[16] = f[15] + (T(1.0) / T(6.0)) * rho * (-vy + vz) - Nyz;
+    } else if (kind == LBM_BC_PRESS_POSY) {
+        T vy = T(1) - (T(1.0) / rho) * (f[0] + f[1] + f[4] + f[5] + f[8] + f[9] + f[12] + f[13] + f[18] +
+                                        T(2.0) * (f[3] + f[7] + f[11] + f[16] + f[17]));
+        T Nyx = T(0.5) * (f[0] + f[8] + f[9] - (f[1] + f[12] + f[13])) - (T(1.0) / T(3.0)) * rho * vx;
+        T Nyz = T(0.5) * (f[4] + f[8] + f[12] - (f[5] + f[9] + f[13])) - (T(1.0) / T(3.0)) * rho * vz;
+        f[2] = f[3] + (T(1.0) / T(3.0)) * rho * vy;
+        f[6] = f[11] + (T(1.0) / T(6.0)) * rho * (vx + vy) - Nyx;
+        f[10] = f[7] + (T(1.0) / T(6.0)) * rho * (-vx + vy) + Nyx;
+        f[14] = f[17] + (T(1.0) / T(6.0)) * rho * (vy + vz) - Nyz;
+        f[15] = f[16] + (T(1.0) / T(6.0)) * rho * (vy - vz) + Nyz;
+    } else if (kind == LBM_BC_PRESS_POSX) {
+        const T vy = vy0;
+        T ux = T(1) - (T(1.0) / rho) * (f[2] + f[3] + f[4] + f[5] + f[14] + f[15] + f[16] + f[17] + f[18] +
+                                        T(2.0) * (f[1] + f[10] + f[11] + f[12] + f[13]));
+        T Nxy = T(0.5) * (f[2] + f[14] + f[15] - (f[3] + f[16] + f[17])) - (T(1.0) / T(3.0)) * rho * vy;
+        T Nxz = T(0.5) * (f[4] + f[10] + f[14] - (f[5] + f[15] + f[17])) - (T(1.0) / T(3.0)) * rho * vz;
+        f[0] = f[1] + (T(1.0) / T(3.0)) * rho * ux;
+        f[7] = f[10] + (T(1.0) / T(6.0)) * rho * (ux - vy) + Nxy;
+        f[6] = f[11] + (T(1.0) / T(6.0)) * rho * (ux + vy) - Nxy;
+        f[8] = f[13] + (T(1.0) / T(6.0)) * rho * (ux + vz) - Nxz;
+        f[9] = f[12] + (T(1.0) / T(6.0)) * rho * (ux - vz) + Nxz;
+    } else if (kind == LBM_BC_PRESS_POSZ) {
+        const T vy = vy0;
+        T uz = T(1) - (T(1.0) / rho) * (f[0] + f[1] + f[2] + f[3] + f[6] + f[7] + f[10] + f[11] + f[18] +
+                                        T(2.0) * (f[5] + f[9] + f[13] + f[15] + f[17]));
+        T Nzx = T(0.5) * (f[0] + f[6] + f[7] - (f[1] + f[10] + f[11])) - (T(1.0) / T(3.0)) * rho * vx;
+        T Nzy = T(0.5) * (f[2] + f[6] + f[10] - (f[3] + f[7] + f[11])) - (T(1.0) / T(3.0)) * rho * vy;
+        f[4] = f[5] + (T(1.0) / T(3.0)) * rho * uz;
+        f[8] = f[13] + (T(1.0) / T(6.0)) * rho * (uz + vx) - Nzx;
+        f[12] = f[9] + (T(1.0) / T(6.0)) * rho * (uz - vx) + Nzx;
+        f[14] = f[17] + (T(1.0) / T(6.0)) * rho * (uz + vy) - Nzy;
+        f[16] = f[15] + (T(1.0) / T(6.0)) * rho * (uz - vy) + Nzy;
+    }
+}
+
+// rho and u from plain populations with the reference's grouped sums
+// (Simulation.cpp:32-79 for D3Q19, :82-148 for D3Q27).
+template <int Q, class T>
+__device__ __forceinline__ void macro_ref(const T* f, T& rho, T& ux, T& uy, T& uz) {
+    rho = T(0.0);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) rho += f[q];
+    if constexpr (Q == 19) {
+        ux = ((f[0] + f[6] + f[7] + f[8] + f[9]) - (f[1] + f[10] + f[11] + f[12] + f[13])) / rho;
+        uy = ((f[2] + f[6] + f[10] + f[14] + f[15]) - (f[3] + f[7] + f[11] + f[16] + f[17])) / rho;
+        uz = ((f[4] + f[8] + f[12] + f[14] + f[16]) - (f[5] + f[9] + f[13] + f[15] + f[17])) / rho;
+    } else {
+        ux = ((f[1] + f[7] + f[8] + f[11] + f[13] + f[19] + f[21] + f[23] + f[25]) -
+              (f[2] + f[9] + f[10] + f[12] + f[14] + f[20] + f[22] + f[24] + f[26])) / rho;
+        uy = ((f[3] + f[7] + f[9] + f[15] + f[16] + f[19] + f[21] + f[24] + f[26]) -
+              (f[4] + f[8] + f[10] + f[17] + f[18] + f[20] + f[22] + f[23] + f[25])) / rho;
+        uz = ((f[5] + f[11] + f[12] + f[15] + f[17] + f[19] + f[22] + f[23] + f[26]) -
+              (f[6] + f[13] + f[14] + f[16] + f[18] + f[20] + f[21] + f[24] + f[25])) / rho;
+    }
+}
+
+// BGK collision.  F64: the reference's expressions.  FP32: shifted form.
+template <int Q, int S>
+__device__ __forceinline__ void collide(typename Work<S>::T* f, const InstParam& ip) {
+    using L = Lat<Q>;
+    if constexpr (S == ST_F64) {
+        double rho, ux, uy, uz;
+        macro_ref<Q, double>(f, rho, ux, uy, uz);
+        const double om = ip.omega;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const double du = ux * (double)L::cx(q) + uy * (double)L::cy(q) + uz * (double)L::cz(q);
+            const double usq = ux * ux + uy * uy + uz * uz;
+            const double feq = L::w(q) * rho * (1.0 + 3.0 * du + 9.0 / 2.0 * du * du - 3.0 / 2.0 * usq);
+            f[q] = om * feq + (1.0 - om) * f[q];
+        }
+    } else {
+        float drho = 0.f, jx = 0.f, jy = 0.f, jz = 0.f;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            drho += f[q];
+            if (L::cx(q)) jx += L::cx(q) > 0 ? f[q] : -f[q];
+            if (L::cy(q)) jy += L::cy(q) > 0 ? f[q] : -f[q];
+            if (L::cz(q)) jz += L::cz(q) > 0 ? f[q] : -f[q];
+        }
+        const float rho = 1.0f + drho;
+        const float inv = 1.0f / rho;
+        const float ux = jx * inv, uy = jy * inv, uz = jz * inv;
+        const float usq15 = 1.5f * (ux * ux + uy * uy + uz * uz);
+        const float om = ip.omega_f;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            float cu = 0.f;
+            if (L::cx(q)) cu += L::cx(q) > 0 ? ux : -ux;
+            if (L::cy(q)) cu += L::cy(q) > 0 ? uy : -uy;
+            if (L::cz(q)) cu += L::cz(q) > 0 ? uz : -uz;
+            const float feqs = (float)L::w(q) * (drho + rho * (cu * (3.0f + 4.5f * cu) - usq15));
+            f[q] = f[q] + om * (feqs - f[q]);
+        }
+    }
+}
+
+// Source (x - c_q) of population q for lane t of a chunk: node id, or -1.
+template <int Q>
+__device__ __forceinline__ int64_t src_index(const int32_t* base, const uint64_t* mask, int lane, int q) {
+    using L = Lat<Q>;
+    const int d = (1 - L::cx(q)) * 3 + (1 - L::cy(q));
+    const int b = lane - L::cz(q) + 1;
+    const uint64_t m = mask[d];
+    if (!((m >> b) & 1ull)) return -1;
+    return (int64_t)base[d] + __popcll(m & ((1ull << b) - 1ull));
+}
+
+struct Partials {
+    double* mass;      // per block
+    double* inflow;
+    double* outflow;
+    double* maxu;
+    int32_t* bad;
+};
+
+template <int Q, int S, int MODE, bool DRY>
+__global__ void __launch_bounds__(512) k_step(StepArgs a, Partials part) {
+    using L = Lat<Q>;
+    using T = typename Work<S>::T;
+    const int lane = threadIdx.x & 31;
+    const int64_t ci = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    double m_mass = 0.0, m_in = 0.0, m_out = 0.0, m_maxu = 0.0;
+    int m_bad = 0;
+    if (ci < a.nchunks) {
+        const Chunk* cp = a.chunks + ci;
+        const int32_t n0 = __ldg(&cp->n0);
+        const uint32_t li = __ldg(&cp->len_inst);
+        const uint32_t wmask = __ldg(&cp->wmask), zmask = __ldg(&cp->zmask);
+        int32_t base[9];
+        uint64_t mask[9];
+#pragma unroll
+        for (int d = 0; d < 9; ++d) { base[d] = __ldg(&cp->base[d]); mask[d] = __ldg(&cp->mask[d]); }
+        const int len = (int)(li & 0xffu);
+        const int inst = (int)(li >> 8);
+        if (lane < len) {
+            const int64_t n = (int64_t)n0 + lane;
+            T f[Q];
+            uint32_t missing = 0;
+            const void* A = a.src;
+#pragma unroll
+            for (int q = 0; q < Q; ++q) {
+                const int64_t s = src_index<Q>(base, mask, lane, q);
+                if (s < 0) missing |= 1u << q;
+                if constexpr (MODE == MODE_PULL) {
+                    f[q] = s >= 0 ? ld<S, Q, true>(A, a.stride, q, s) : T(0);
+                } else if constexpr (MODE == MODE_AA_EVEN) {
+                    f[q] = ld<S, Q>(A, a.stride, q, n);
+                } else {
+                    f[q] = s >= 0 ? ld<S, Q>(A, a.stride, L::opp(q), s) : T(0);
+                }
+            }
+            if (missing) {
+                const bool wall = (wmask >> lane) & 1u;
+#pragma unroll
+                for (int q = 0; q < Q; ++q) {
+                    if (!((missing >> q) & 1u)) continue;
+                    if (wall && q != L::NO_BB_POP) {
+                        if constexpr (MODE == MODE_PULL) f[q] = ld<S, Q, true>(A, a.stride, L::opp(q), n);
+                        else if constexpr (MODE == MODE_AA_ODD) f[q] = ld<S, Q>(A, a.stride, q, n);
+                        // AA_EVEN: slot q of x already holds f*_{opp q}(x)
+                    } else {
+                        f[q] = S == ST_F64 ? T(L::w(q)) : T(0);
+                    }
+                }
+            }
+            const int64_t step = a.step + (a.step_base ? *a.step_base : 0);
+            bool zl = (zmask >> lane) & 1u;
+            int zkind = 0;
+            double zdir = 0.0;
+            if (zl) {
+                const int slot = __ldg(&cp->zslot0) + __popc(zmask & ((1u << lane) - 1u));
+                const ZSlot z = a.zslots[slot];
+                const ListParam lp = a.lists[z.list];
+                zkind = z.kind;
+                T p[Q];
+#pragma unroll
+                for (int q = 0; q < Q; ++q) p[q] = plain<S, Q>(f[q], q);
+                if (z.kind == LBM_BC_VEL_NEGY || z.kind == LBM_BC_VEL_POSX) {
+                    const double amp = a.amp[lp.amp_off + step % lp.amp_len];
+                    const double sc = amp * z.profile;
+                    const T v[3] = {T(sc * lp.dir[0]), T(sc * lp.dir[1]), T(sc * lp.dir[2])};
+                    if constexpr (Q == 19) {
+                        if (z.kind == LBM_BC_VEL_NEGY) zh_vel_negy<T>(p, v);
+                    } else {
+                        if (z.kind == LBM_BC_VEL_POSX) zh_vel_posx_q27<T>(p, v);
+                    }
+                    zdir = 1.0;
+                } else {
+                    if constexpr (Q == 19) zh_press<T>(p, z.kind, T(lp.rho));
+                    zdir = -1.0;
+                }
+#pragma unroll
+                for (int q = 0; q < Q; ++q) f[q] = unplain<S, Q>(p[q], q);
+            }
+            if constexpr (DRY) {
+                double fp[Q];
+#pragma unroll
+                for (int q = 0; q < Q; ++q) fp[q] = (double)plain<S, Q>(f[q], q);
+                double rho, ux, uy, uz;
+                macro_ref<Q, double>(fp, rho, ux, uy, uz);
+                if (a.out_f) {
+#pragma unroll
+                    for (int q = 0; q < Q; ++q) a.out_f[n * Q + q] = fp[q];
+                }
+                if (a.out_rho) a.out_rho[n] = rho;
+                if (a.out_u) { a.out_u[3 * n] = ux; a.out_u[3 * n + 1] = uy; a.out_u[3 * n + 2] = uz; }
+                const double sp = sqrt(ux * ux + uy * uy + uz * uz);
+                m_mass = rho;
+                m_maxu = sp;
+                m_bad = (isfinite(rho) && isfinite(sp)) ? 0 : 1;
+                if (zl) {
+                    if (zdir > 0) m_in = rho * sp;
+                    else m_out = rho * sp;
+                }
+                (void)zkind;
+            } else {
+                collide<Q, S>(f, a.insts[inst]);
+                void* D = a.dst;
+#pragma unroll
+                for (int q = 0; q < Q; ++q) {
+                    if constexpr (MODE == MODE_PULL) {
+                        st<S, Q>(D, a.stride, q, n, f[q]);
+                    } else if constexpr (MODE == MODE_AA_EVEN) {
+                        st<S, Q>(D, a.stride, L::opp(q), n, f[q]);
+                    } else {
+                        if ((missing >> L::opp(q)) & 1u) {
+                            st<S, Q>(D, a.stride, L::opp(q), n, f[q]);
+                        } else {
+                            const int64_t d = src_index<Q>(base, mask, lane, L::opp(q));
+                            st<S, Q>(D, a.stride, q, d, f[q]);
+                        }
+                    }
+                }
+            }
+        }
+    }
+    if constexpr (DRY) {
+        if (part.mass) {
+            // deterministic block reduction: warp shuffles then warp 0
+            __shared__ double sm[4][16];
+            __shared__ int sb[16];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                m_mass += __shfl_down_sync(0xffffffffu, m_mass, o);
+                m_in += __shfl_down_sync(0xffffffffu, m_in, o);
+                m_out += __shfl_down_sync(0xffffffffu, m_out, o);
+                m_maxu = fmax(m_maxu, __shfl_down_sync(0xffffffffu, m_maxu, o));
+                m_bad |= __shfl_down_sync(0xffffffffu, m_bad, o);
+            }
+            const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+            if (lane == 0) { sm[0][w] = m_mass; sm[1][w] = m_in; sm[2][w] = m_out; sm[3][w] = m_maxu; sb[w] = m_bad; }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                double s0 = 0, s1 = 0, s2 = 0, s3 = 0;
+                int b = 0;
+                for (int i = 0; i < nw; ++i) { s0 += sm[0][i]; s1 += sm[1][i]; s2 += sm[2][i]; s3 = fmax(s3, sm[3][i]); b |= sb[i]; }
+                part.mass[blockIdx.x] = s0; part.inflow[blockIdx.x] = s1; part.outflow[blockIdx.x] = s2;
+                part.maxu[blockIdx.x] = s3; part.bad[blockIdx.x] = b;
+            }
+        }
+    }
+}
+
+}  // namespace lbm
