@@ -27,11 +27,12 @@ OUTLET_LIST = 2   # the reference's outlet list 2 carries the +y-unknown pressur
 
 @dataclass
 class Inlet:
-    center: tuple          # (x, z) of the axis at the inlet plane
+    center: tuple          # coordinates of the vessel axis on the two other axes (ascending axis order)
     radius: float
-    plane: float           # y of the inlet lattice plane
+    plane: float           # coordinate of the inlet lattice plane
     u_max: float
     period: int = 0        # pulsation period in steps (0 = steady)
+    axis: int = 1          # axis normal to the inlet face
 
 
 @dataclass
@@ -52,9 +53,16 @@ class Case:
 
     def inlet_profile(self, geom):
         """Parabolic factor 1 - r^2/R^2 (>= 0) of each inlet-list point, list order."""
-        pts = geom.coords(geom.list(INLET_LIST))
-        cx, cz = self.inlet.center
-        r2 = (pts[:, 0] - cx) ** 2 + (pts[:, 2] - cz) ** 2
+        return self.inlet_profile_from_indices(geom.list(INLET_LIST), geom.GeomSize)
+
+    def inlet_profile_from_indices(self, idx, dims):
+        Nx, Ny, Nz = (int(v) for v in dims)
+        idx = np.asarray(idx, dtype=np.int64)
+        ijk = np.stack([idx // (Ny * Nz), (idx // Nz) % Ny, idx % Nz], axis=1).astype(np.float64)
+        mn = np.asarray(self.grid[0], dtype=np.float64)
+        pts = mn + ijk * self.spacing
+        others = [a for a in range(3) if a != self.inlet.axis]
+        r2 = (pts[:, others[0]] - self.inlet.center[0]) ** 2 + (pts[:, others[1]] - self.inlet.center[1]) ** 2
         return np.maximum(0.0, 1.0 - r2 / self.inlet.radius ** 2)
 
     def amp_table(self):
@@ -92,6 +100,24 @@ def pipe(radius=20.0, length=120.0, segments=64, ny=128, nxz=48, tau=0.8, u_max=
     return Case("pipe", tris, ((0.0, 0.0, 0.0), (nxz, ny, nxz)), preds,
                 Inlet((c[0], c[2]), radius, inlet_plane, u_max), tau, steps,
                 meta={"radius": radius, "length": length, "segments": segments})
+
+
+def pipe_x(radius=12.0, length=80.0, segments=48, nx=88, nyz=32, tau=0.8, u_max=0.04, steps=200):
+    """Straight cylinder along x with the inlet on the x-min face: the orientation of
+    the reference's D3Q27 velocity routine (unknowns +x, Boundary.cpp:87-123).  The
+    x-max face carries an outlet predicate (list 2) for lattices that have one."""
+    c = ((nx - 1) / 2.0, (nyz - 1) / 2.0, (nyz - 1) / 2.0)
+    tris = synth_cylinder(radius, length, segments, 0, c)
+    x_lo, x_hi = c[0] - length / 2.0, c[0] + length / 2.0
+    inlet_plane, outlet_plane = math.ceil(x_lo), math.floor(x_hi)
+    half = radius + 3
+    preds = [PlanePredicate(INLET_LIST, 0, float(inlet_plane), 1e-2, (math.nan, c[1] - half, c[2] - half),
+                            (math.nan, c[1] + half, c[2] + half)),
+             PlanePredicate(OUTLET_LIST, 0, float(outlet_plane), 1e-2, (math.nan, c[1] - half, c[2] - half),
+                            (math.nan, c[1] + half, c[2] + half))]
+    return Case("pipe_x", tris, ((0.0, 0.0, 0.0), (nx, nyz, nyz)), preds,
+                Inlet((c[1], c[2]), radius, inlet_plane, u_max, 0, axis=0), tau, steps,
+                meta={"radius": radius, "length": length})
 
 
 def bifurcation(nx=256, ny=512, nz=256, r_parent=24.0, r_child=18.0, angle_deg=30.0, h=1.8, seed=0xB1F,

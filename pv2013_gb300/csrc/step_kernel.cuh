@@ -300,8 +300,11 @@ __global__ void __launch_bounds__(512) k_step(StepArgs a, Partials part) {
                     }
                 }
             }
+            // launch n turns f*(n-1) into f_n: its boundary conditions are those of
+            // reference iteration n-1 (Simulation.cpp:913-915); f_0 is the initial
+            // state, which the reference collides before any boundary condition
             const int64_t step = a.step + (a.step_base ? *a.step_base : 0);
-            bool zl = (zmask >> lane) & 1u;
+            const bool zl = ((zmask >> lane) & 1u) && step > 0;
             int zkind = 0;
             double zdir = 0.0;
             if (zl) {
@@ -313,7 +316,7 @@ __global__ void __launch_bounds__(512) k_step(StepArgs a, Partials part) {
 #pragma unroll
                 for (int q = 0; q < Q; ++q) p[q] = plain<S, Q>(f[q], q);
                 if (z.kind == LBM_BC_VEL_NEGY || z.kind == LBM_BC_VEL_POSX) {
-                    const double amp = a.amp[lp.amp_off + step % lp.amp_len];
+                    const double amp = a.amp[lp.amp_off + (step - 1) % lp.amp_len];
                     const double sc = amp * z.profile;
                     const T v[3] = {T(sc * lp.dir[0]), T(sc * lp.dir[1]), T(sc * lp.dir[2])};
                     if constexpr (Q == 19) {
