@@ -198,7 +198,10 @@ typedef struct lbm_sim_params {
     double tau;                /* relaxation time; omega = 1/tau (Simulation.cpp:11) */
     const lbm_list_bc* bcs;
     size_t nbcs;
-    int32_t warps_per_block;   /* 0 = default / autotuned */
+    int32_t warps_per_block;   /* 1..8; 0 = default / autotuned */
+    int32_t run_axis;          /* node numbering axis (chunks are runs along it):
+                                  1 = y, 2 = z (the reference's x-major order),
+                                  0 = the one giving fewer chunks */
 } lbm_sim_params;
 
 typedef struct lbm_sim lbm_sim;
@@ -226,7 +229,7 @@ typedef struct lbm_sim_info {
     int64_t n_instances;
     int64_t steps_done;
     int64_t n_chunks;
-    int32_t Q, precision, pattern, warps_per_block;
+    int32_t Q, precision, pattern, warps_per_block, run_axis;
     int64_t state_bytes;       /* device bytes of the population arrays */
     double algorithmic_bytes_per_update;  /* 2*Q*storage bytes */
 } lbm_sim_info;

@@ -68,22 +68,32 @@ template <> struct Lat<27> {
 };
 
 // ---------------------------------------------------------------------------
-// Run-table lattice: fluid nodes are numbered in x-major order (z fastest);
-// each z-run of a grid column is cut into chunks of at most 32 nodes, one warp
-// per chunk.  For the nine columns (i+di, j+dj), di,dj in {-1,0,1}, a chunk
-// holds a fluid bit mask over the window k0-1 .. k0+32 (bit b <-> k0-1+b) and
-// the node id of the lowest fluid point of that window, so the node id of any
-// neighbour of lane t is base + popcount(mask below its bit).
+// Run-table lattice.  Fluid nodes are numbered with the run axis fastest
+// (z for the reference's x-major order; y when the vessels run along y);
+// each run of consecutive fluid points along that axis is cut into chunks of
+// at most 32 nodes, one warp per chunk.  The two other axes (a, b) span the
+// grid columns.  For the eight neighbouring columns (a+da, b+db) a chunk
+// holds a fluid bit mask over the window r0-1 .. r0+32 along the run axis
+// (bit p <-> r0-1+p) and the node id of the lowest fluid point of that window,
+// so the node id of a neighbour of lane t is base + popcount(mask below its
+// bit).  The chunk's own column is a run: only its two end bits are stored.
 struct __align__(128) Chunk {
     int32_t n0;        // node id of lane 0
-    uint32_t len_inst; // bits 0-7: number of nodes (1..32); bits 8-31: instance
+    uint32_t len_inst; // bits 0-5: nodes (1..32); bit 6: own column fluid at r0-1;
+                       // bit 7: own column fluid at r0+len; bits 8-31: instance
     uint32_t wmask;    // lanes that are wall nodes (bounce-back)
     uint32_t zmask;    // lanes that carry a Zou-He boundary condition
-    int32_t zslot0;    // Zou-He slot of the first such lane
-    int32_t base[9];   // column (di,dj) -> index (di+1)*3 + (dj+1)
-    uint64_t mask[9];
+    uint32_t bmask;    // lanes that are boundary nodes (may miss a neighbour)
+    int32_t zslot0;    // Zou-He slot of the first zmask lane
+    int32_t base[8];   // neighbour columns, index col8(da, db)
+    uint64_t mask[8];
 };
 static_assert(sizeof(Chunk) == 128, "chunk descriptor is one 128-byte line");
+
+// (da, db) in {-1,0,1}^2 minus (0,0) -> 0..7
+__host__ __device__ constexpr int col8(int da, int db) {
+    return (da + 1) * 3 + (db + 1) - ((da + 1) * 3 + (db + 1) > 4 ? 1 : 0);
+}
 
 // Zou-He slot of one boundary node.
 struct ZSlot {
@@ -136,6 +146,7 @@ struct StepArgs {
     double* out_f;
     double* out_rho;
     double* out_u;
+    const int32_t* out_pos;   // output position of each node (x-major rank), or null = identity
     int64_t n_nodes;
 };
 

@@ -79,11 +79,50 @@ __global__ void k_scatter_ids(const int64_t* __restrict__ node_grid, int64_t n, 
         node_of_point[node_grid[i]] = (int32_t)i;
 }
 
+// Grid permutation for the run axis.  Permuted layout: index (a*Nb + b)*Nr + r
+// with r the run axis; for run axis z it is the x-major layout itself, for
+// run axis y it is (x*Nz + z)*Ny + y.
+struct Perm {
+    int ra;             // 1 (y) or 2 (z)
+    int Nx, Ny, Nz;
+    __host__ __device__ int Na() const { return Nx; }
+    __host__ __device__ int Nb() const { return ra == 2 ? Ny : Nz; }
+    __host__ __device__ int Nr() const { return ra == 2 ? Nz : Ny; }
+    __host__ __device__ int64_t to_perm(int64_t o) const {
+        if (ra == 2) return o;
+        const int64_t k = o % Nz, t = o / Nz, j = t % Ny, i = t / Ny;
+        return (i * Nz + k) * Ny + j;
+    }
+    __host__ __device__ int64_t to_orig(int64_t p) const {
+        if (ra == 2) return p;
+        const int64_t j = p % Ny, t = p / Ny, k = t % Nz, i = t / Nz;
+        return (i * Ny + j) * Nz + k;
+    }
+};
+
+__global__ void k_permute_flags(const uint8_t* __restrict__ in, Perm P, uint8_t* __restrict__ out) {
+    const int64_t n = (int64_t)P.Nx * P.Ny * P.Nz;
+    for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < n; o += (int64_t)gridDim.x * blockDim.x)
+        out[P.to_perm(o)] = in[o];
+}
+
+__global__ void k_to_orig(int64_t* __restrict__ idx, int64_t n, Perm P) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        idx[i] = P.to_orig(idx[i]);
+}
+
+// out_pos[n] = node_off + x-major rank of node n (rank_of_point holds the rank of each fluid point)
+__global__ void k_xrank(const int64_t* __restrict__ node_orig, int64_t n, const int32_t* __restrict__ rank_of_point,
+                        int64_t node_off, int32_t* __restrict__ pos) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        pos[i] = (int32_t)(node_off + rank_of_point[node_orig[i]]);
+}
+
 // role: 0 interior, 1 wall, 2+l first matching predicate list l
-__global__ void k_roles(const int64_t* __restrict__ bidx, const uint64_t* __restrict__ bmask, int64_t nb,
+__global__ void k_roles(const int64_t* __restrict__ bidx, const uint64_t* __restrict__ bmask, int64_t nb, Perm P,
                         const int32_t* __restrict__ node_of_point, int8_t* __restrict__ role) {
     for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < nb; b += (int64_t)gridDim.x * blockDim.x) {
-        const int32_t n = node_of_point[bidx[b]];
+        const int32_t n = node_of_point[P.to_perm(bidx[b])];
         const uint64_t m = bmask[b];
         role[n] = m ? (int8_t)(2 + __ffsll((long long)m) - 1) : (int8_t)1;
     }
@@ -102,15 +141,15 @@ __global__ void k_gather_role(const int64_t* __restrict__ ids, int64_t n, const 
         out[i] = role[ids[i]];
 }
 
-// chunks per grid column
-__global__ void k_col_count(const uint8_t* __restrict__ flags, int Nx, int Ny, int Nz, int32_t* __restrict__ cnt) {
-    const int64_t ncol = (int64_t)Nx * Ny;
+// chunks per grid column (permuted layout, runs along the last axis)
+__global__ void k_col_count(const uint8_t* __restrict__ flags, int Na, int Nb, int Nr, int32_t* __restrict__ cnt) {
+    const int64_t ncol = (int64_t)Na * Nb;
     for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncol; c += (int64_t)gridDim.x * blockDim.x) {
-        const uint8_t* f = flags + c * Nz;
+        const uint8_t* f = flags + c * Nr;
         int32_t n = 0;
         int run = 0;
-        for (int k = 0; k <= Nz; ++k) {
-            const bool fl = k < Nz && f[k];
+        for (int k = 0; k <= Nr; ++k) {
+            const bool fl = k < Nr && f[k];
             if (fl) ++run;
             if (!fl || run == 32) {
                 if (run > 0) ++n;
@@ -122,10 +161,10 @@ __global__ void k_col_count(const uint8_t* __restrict__ flags, int Nx, int Ny, i
 }
 
 struct FillArgs {
-    const uint8_t* flags;
-    int Nx, Ny, Nz;
+    const uint8_t* flags;         // permuted layout
+    int Na, Nb, Nr;
     const int64_t* chunk_off;     // per column
-    const int32_t* node_of_point; // local ids
+    const int32_t* node_of_point; // local ids, permuted layout
     const int8_t* role;
     const int64_t* znodes;        // sorted local ids of Zou-He nodes
     int64_t nz;
@@ -144,26 +183,30 @@ __device__ int64_t lower_bound_i64(const int64_t* a, int64_t n, int64_t v) {
 }
 
 __global__ void k_col_fill(FillArgs A) {
-    const int64_t ncol = (int64_t)A.Nx * A.Ny;
+    const int64_t ncol = (int64_t)A.Na * A.Nb;
     for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncol; c += (int64_t)gridDim.x * blockDim.x) {
-        const int i = (int)(c / A.Ny), j = (int)(c % A.Ny);
-        const uint8_t* f = A.flags + c * A.Nz;
+        const int i = (int)(c / A.Nb), j = (int)(c % A.Nb);
+        const uint8_t* f = A.flags + c * A.Nr;
         int64_t out = A.chunk_off[c];
         int run = 0, k0 = 0;
-        for (int k = 0; k <= A.Nz; ++k) {
-            const bool fl = k < A.Nz && f[k];
+        for (int k = 0; k <= A.Nr; ++k) {
+            const bool fl = k < A.Nr && f[k];
             if (fl) { if (run == 0) k0 = k; ++run; }
             if (!fl || run == 32) {
                 if (run > 0) {
                     Chunk ch;
-                    const int32_t n0 = A.node_of_point[c * A.Nz + k0];
+                    const int32_t n0 = A.node_of_point[c * A.Nr + k0];
+                    const uint32_t e0 = (k0 > 0 && f[k0 - 1]) ? 1u : 0u;
+                    const uint32_t e1 = (k0 + run < A.Nr && f[k0 + run]) ? 1u : 0u;
                     ch.n0 = (int32_t)(A.node_off + n0);
-                    ch.len_inst = (uint32_t)run | ((uint32_t)A.inst << 8);
+                    ch.len_inst = (uint32_t)run | (e0 << 6) | (e1 << 7) | ((uint32_t)A.inst << 8);
                     ch.wmask = 0;
                     ch.zmask = 0;
+                    ch.bmask = 0;
                     for (int t = 0; t < run; ++t) {
                         const int r = A.role[n0 + t];
                         if (r == 1) ch.wmask |= 1u << t;
+                        if (r >= 1) ch.bmask |= 1u << t;
                     }
                     const int64_t zfirst = lower_bound_i64(A.znodes, A.nz, n0);
                     ch.zslot0 = (int32_t)(A.zslot_off + zfirst);
@@ -171,22 +214,23 @@ __global__ void k_col_fill(FillArgs A) {
                         ch.zmask |= 1u << (int)(A.znodes[zz] - n0);
                     for (int di = -1; di <= 1; ++di)
                         for (int dj = -1; dj <= 1; ++dj) {
-                            const int d = (di + 1) * 3 + (dj + 1);
+                            if (di == 0 && dj == 0) continue;
+                            const int d = col8(di, dj);
                             const int a = i + di, b = j + dj;
                             uint64_t m = 0;
                             int32_t base = 0;
-                            if (a >= 0 && a < A.Nx && b >= 0 && b < A.Ny) {
-                                const int64_t cc = (int64_t)a * A.Ny + b;
-                                const uint8_t* g = A.flags + cc * A.Nz;
+                            if (a >= 0 && a < A.Na && b >= 0 && b < A.Nb) {
+                                const int64_t cc = (int64_t)a * A.Nb + b;
+                                const uint8_t* g = A.flags + cc * A.Nr;
                                 int first = -1;
                                 for (int bit = 0; bit < 34; ++bit) {
                                     const int kk = k0 - 1 + bit;
-                                    if (kk >= 0 && kk < A.Nz && g[kk]) {
+                                    if (kk >= 0 && kk < A.Nr && g[kk]) {
                                         m |= 1ull << bit;
                                         if (first < 0) first = kk;
                                     }
                                 }
-                                if (first >= 0) base = (int32_t)(A.node_off + A.node_of_point[cc * A.Nz + first]);
+                                if (first >= 0) base = (int32_t)(A.node_off + A.node_of_point[cc * A.Nr + first]);
                             }
                             ch.mask[d] = m;
                             ch.base[d] = base;
@@ -265,7 +309,7 @@ int store_bytes(int s) { return s == ST_F64 ? 8 : (s == ST_F32 ? 4 : 2); }
 
 struct lbm_sim {
     int dev = 0;
-    int Q = 19, store = ST_F64, pattern = LBM_PULL, wpb = 4;
+    int Q = 19, store = ST_F64, pattern = LBM_PULL, wpb = 4, ra = 2;
     int64_t N = 0, nchunks = 0, stride = 0, nz = 0;
     int64_t n_inst = 0;
     void* buf[2] = {nullptr, nullptr};
@@ -275,14 +319,14 @@ struct lbm_sim {
     ListParam* lists = nullptr;
     InstParam* insts = nullptr;
     double* amp = nullptr;
-    int64_t* node_grid = nullptr;  // grid index per node (per instance)
+    int64_t* node_grid = nullptr;  // x-major grid index of each output node (per instance, x-major order)
+    int32_t* out_pos = nullptr;    // output position (x-major rank) of each internal node; null = identity
     std::vector<int64_t> inst_off; // node offsets, n_inst + 1
     int64_t steps_done = 0;
     // graph replay
     cudaGraphExec_t gexec = nullptr;
     cudaGraph_t graph = nullptr;
     int64_t glen = 0;
-    int gcur = 0;
     int64_t* step_base = nullptr;
     // monitors
     double* part = nullptr;        // 4 * nblocks doubles
@@ -297,34 +341,80 @@ namespace {
 
 struct InstBuild {
     int64_t N = 0;
-    DBuf<int64_t> node_grid;
+    DBuf<int64_t> node_grid;       // x-major grid indices, x-major order
+    DBuf<int32_t> out_pos;         // when the run axis is not z
     DBuf<Chunk> chunks;
     int64_t nchunks = 0;
     std::vector<ZSlot> zslots;
 };
 
-lbm_status build_instance(const lbm_geometry* g, const lbm_sim_params* p, int32_t inst, int64_t node_off,
+// Chunk count of a geometry for a run axis (set-up heuristic for run_axis 0).
+lbm_status count_chunks(const lbm_geometry* g, int ra, cudaStream_t st, int64_t* n) {
+    int dims[3];
+    geometry_dims(g, dims);
+    const Perm P{ra, dims[0], dims[1], dims[2]};
+    const int64_t npts = (int64_t)dims[0] * dims[1] * dims[2];
+    const uint8_t* flags = geometry_flags_dev(g);
+    DBuf<uint8_t> fp;
+    if (ra != 2) {
+        LBM_TRY(fp.alloc(npts, "permuted flags"));
+        k_permute_flags<<<blocks_for(npts, 256), 256, 0, st>>>(flags, P, fp.p);
+        flags = fp.p;
+    }
+    const int64_t ncol = (int64_t)P.Na() * P.Nb();
+    DBuf<int32_t> cc;
+    DBuf<int64_t> co;
+    LBM_TRY(cc.alloc(ncol, "chunk counts"));
+    LBM_TRY(co.alloc(ncol, "chunk offsets"));
+    k_col_count<<<blocks_for(ncol, 128), 128, 0, st>>>(flags, P.Na(), P.Nb(), P.Nr(), cc.p);
+    return scan::exclusive_scan(cc.p, ncol, co.p, n, st);
+}
+
+lbm_status build_instance(const lbm_geometry* g, const lbm_sim_params* p, int32_t inst, int ra, int64_t node_off,
                           int64_t zslot_off, cudaStream_t st, InstBuild& out) {
     int dims[3];
     geometry_dims(g, dims);
+    const Perm P{ra, dims[0], dims[1], dims[2]};
     const int64_t npts = (int64_t)dims[0] * dims[1] * dims[2];
     const uint8_t* flags = geometry_flags_dev(g);
-    // 1. node numbering (x-major compaction of Fluid points)
+    DBuf<uint8_t> fperm;
+    const uint8_t* pflags = flags;
+    if (ra != 2) {
+        LBM_TRY(fperm.alloc(npts, "permuted flags"));
+        k_permute_flags<<<blocks_for(npts, 256), 256, 0, st>>>(flags, P, fperm.p);
+        pflags = fperm.p;
+    }
+    // 1. node numbering: compaction of Fluid points in the permuted order
     int64_t* ng = nullptr;
-    LBM_TRY(scan::compact(flags, npts, &ng, &out.N, st));
-    out.node_grid.p = ng;
+    LBM_TRY(scan::compact(pflags, npts, &ng, &out.N, st));
+    DBuf<int64_t> node_perm; node_perm.p = ng;
     if (out.N == 0) return fail(LBM_ERR_ARG, "instance %d has no fluid node", inst);
     if (node_off + out.N >= INT32_MAX) return fail(LBM_ERR_ARG, "more than 2^31 nodes");
     DBuf<int32_t> nop;
     LBM_TRY(nop.alloc(npts, "node map"));
     LBM_CUDA(cudaMemsetAsync(nop.p, 0xff, sizeof(int32_t) * npts, st));
     k_scatter_ids<<<blocks_for(out.N, 256), 256, 0, st>>>(ng, out.N, nop.p);
+    // output order: x-major (the reference's node order, Subdomain.cpp:638-651)
+    if (ra == 2) {
+        out.node_grid.p = node_perm.release();
+    } else {
+        int64_t nx = 0;
+        int64_t* xg = nullptr;
+        LBM_TRY(scan::compact(flags, npts, &xg, &nx, st));
+        out.node_grid.p = xg;
+        DBuf<int32_t> rank;
+        LBM_TRY(rank.alloc(npts, "rank map"));
+        k_scatter_ids<<<blocks_for(nx, 256), 256, 0, st>>>(xg, nx, rank.p);
+        k_to_orig<<<blocks_for(out.N, 256), 256, 0, st>>>(node_perm.p, out.N, P);
+        LBM_TRY(out.out_pos.alloc(out.N, "output positions"));
+        k_xrank<<<blocks_for(out.N, 256), 256, 0, st>>>(node_perm.p, out.N, rank.p, node_off, out.out_pos.p);
+    }
     // 2. roles
     DBuf<int8_t> role;
     LBM_TRY(role.alloc(out.N, "node roles"));
     LBM_CUDA(cudaMemsetAsync(role.p, 0, out.N, st));
     const int64_t nb = geometry_nboundary(g);
-    if (nb) k_roles<<<blocks_for(nb, 256), 256, 0, st>>>(geometry_bidx_dev(g), geometry_bmask_dev(g), nb, nop.p, role.p);
+    if (nb) k_roles<<<blocks_for(nb, 256), 256, 0, st>>>(geometry_bidx_dev(g), geometry_bmask_dev(g), nb, P, nop.p, role.p);
     // 3. Zou-He nodes: role list with a boundary-condition kind
     int kind[64] = {0};
     const lbm_list_bc* lbc[64] = {nullptr};
@@ -344,13 +434,33 @@ lbm_status build_instance(const lbm_geometry* g, const lbm_sim_params* p, int32_
     LBM_TRY(scan::compact(zf.p, out.N, &zn, &nzn, st));
     DBuf<int64_t> znodes; znodes.p = zn;
     {
+        // profile values follow the list's x-major order (the reference's
+        // InletBoundaryNode_ order); slots follow the internal node order
         DBuf<int8_t> zr;
         LBM_TRY(zr.alloc(nzn, "zou-he roles"));
         if (nzn) k_gather_role<<<blocks_for(nzn, 256), 256, 0, st>>>(zn, nzn, role.p, zr.p);
         std::vector<int8_t> hr(nzn);
-        if (nzn) LBM_CUDA(cudaMemcpyAsync(hr.data(), zr.p, nzn, cudaMemcpyDeviceToHost, st));
+        std::vector<int64_t> hid(nzn);
+        if (nzn) {
+            LBM_CUDA(cudaMemcpyAsync(hr.data(), zr.p, nzn, cudaMemcpyDeviceToHost, st));
+            if (ra != 2) {
+                std::vector<int32_t> pos(out.N);
+                std::vector<int64_t> ids(nzn);
+                LBM_CUDA(cudaMemcpyAsync(pos.data(), out.out_pos.p, sizeof(int32_t) * out.N, cudaMemcpyDeviceToHost, st));
+                LBM_CUDA(cudaMemcpyAsync(ids.data(), zn, sizeof(int64_t) * nzn, cudaMemcpyDeviceToHost, st));
+                LBM_CUDA(cudaStreamSynchronize(st));
+                for (int64_t s = 0; s < nzn; ++s) hid[s] = pos[ids[s]];
+            } else {
+                LBM_CUDA(cudaMemcpyAsync(hid.data(), zn, sizeof(int64_t) * nzn, cudaMemcpyDeviceToHost, st));
+            }
+        }
         LBM_CUDA(cudaStreamSynchronize(st));
-        std::vector<int64_t> rank(64, 0);
+        // rank of each slot within its list in x-major order
+        std::vector<int64_t> order(nzn);
+        for (int64_t s = 0; s < nzn; ++s) order[s] = s;
+        std::sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return hid[a] < hid[b]; });
+        std::vector<int64_t> rank(64, 0), slot_rank(nzn);
+        for (int64_t s : order) slot_rank[s] = rank[hr[s] - 2]++;
         out.zslots.resize(nzn);
         for (int64_t s = 0; s < nzn; ++s) {
             const int l = hr[s] - 2;
@@ -358,7 +468,7 @@ lbm_status build_instance(const lbm_geometry* g, const lbm_sim_params* p, int32_
             ZSlot z;
             z.list = inst * 64 + l;
             z.kind = kind[l];
-            const int64_t r = rank[l]++;
+            const int64_t r = slot_rank[s];
             z.profile = 1.0;
             if (L && L->profile) {
                 if ((size_t)r >= L->profile_len)
@@ -376,16 +486,16 @@ lbm_status build_instance(const lbm_geometry* g, const lbm_sim_params* p, int32_
         }
     }
     // 4. chunks
-    const int64_t ncol = (int64_t)dims[0] * dims[1];
+    const int64_t ncol = (int64_t)P.Na() * P.Nb();
     DBuf<int32_t> ccount;
     DBuf<int64_t> coff;
     LBM_TRY(ccount.alloc(ncol, "chunk counts"));
     LBM_TRY(coff.alloc(ncol, "chunk offsets"));
-    k_col_count<<<blocks_for(ncol, 128), 128, 0, st>>>(flags, dims[0], dims[1], dims[2], ccount.p);
+    k_col_count<<<blocks_for(ncol, 128), 128, 0, st>>>(pflags, P.Na(), P.Nb(), P.Nr(), ccount.p);
     LBM_TRY(scan::exclusive_scan(ccount.p, ncol, coff.p, &out.nchunks, st));
     LBM_TRY(out.chunks.alloc(out.nchunks, "chunks"));
     FillArgs fa;
-    fa.flags = flags; fa.Nx = dims[0]; fa.Ny = dims[1]; fa.Nz = dims[2];
+    fa.flags = pflags; fa.Na = P.Na(); fa.Nb = P.Nb(); fa.Nr = P.Nr();
     fa.chunk_off = coff.p; fa.node_of_point = nop.p; fa.role = role.p;
     fa.znodes = zn; fa.nz = nzn; fa.node_off = node_off; fa.zslot_off = zslot_off; fa.inst = inst;
     fa.chunks = out.chunks.p;
@@ -402,9 +512,13 @@ lbm_status sim_launch(lbm_sim* S, int mode, bool dry, void* src, void* dst, int6
     a.src = src; a.dst = dst; a.stride = S->stride;
     a.zslots = S->zslots; a.lists = S->lists; a.insts = S->insts; a.amp = S->amp;
     a.step = step; a.step_base = step_base;
-    a.out_f = of; a.out_rho = orho; a.out_u = ou; a.n_nodes = S->N;
-    if (S->store == ST_F64) return launch_step_f64(S->Q, mode, dry, a, part, S->wpb, st);
-    return launch_step_lp(S->Q, S->store, mode, dry, a, part, S->wpb, st);
+    a.out_f = of; a.out_rho = orho; a.out_u = ou; a.out_pos = S->out_pos; a.n_nodes = S->N;
+    switch (S->store) {
+        case ST_F64: return launch_step_f64(S->Q, mode, dry, S->ra, a, part, S->wpb, st);
+        case ST_F32: return launch_step_f32(S->Q, mode, dry, S->ra, a, part, S->wpb, st);
+        case ST_F16S: return launch_step_f16s(S->Q, mode, dry, S->ra, a, part, S->wpb, st);
+        default: return launch_step_bf16s(S->Q, mode, dry, S->ra, a, part, S->wpb, st);
+    }
 }
 
 // Launches one step at the current state; advances cur/steps_done.
@@ -476,7 +590,8 @@ lbm_status sim_create(const lbm_geometry* const* g, const lbm_sim_params* p, siz
     S->pattern = p0.pattern == LBM_AUTO ? LBM_AA : p0.pattern;
     if (S->pattern != LBM_PULL && S->pattern != LBM_AA) return fail(LBM_ERR_ARG, "unknown pattern %d", p0.pattern);
     S->wpb = p0.warps_per_block > 0 ? p0.warps_per_block : 4;
-    if (S->wpb > 16) return fail(LBM_ERR_ARG, "warps_per_block must be <= 16");
+    if (S->wpb > 8) return fail(LBM_ERR_ARG, "warps_per_block must be <= 8");
+    if (p0.run_axis != 0 && p0.run_axis != 1 && p0.run_axis != 2) return fail(LBM_ERR_ARG, "run_axis must be 0, 1 or 2");
     for (size_t i = 0; i < n; ++i) {
         if (p[i].Q != p0.Q || p[i].precision != p0.precision || p[i].pattern != p0.pattern)
             return fail(LBM_ERR_ARG, "batch members must share Q, precision and pattern");
@@ -484,13 +599,26 @@ lbm_status sim_create(const lbm_geometry* const* g, const lbm_sim_params* p, siz
         if (geometry_device(g[i]) != S->dev) return fail(LBM_ERR_ARG, "geometry %zu lives on another device", i);
     }
     S->n_inst = (int64_t)n;
+    if (p0.run_axis != 0) {
+        S->ra = p0.run_axis;
+    } else {
+        int64_t cy = 0, cz = 0;
+        for (size_t i = 0; i < n; ++i) {
+            int64_t a = 0, b = 0;
+            LBM_TRY(count_chunks(g[i], 1, st, &a));
+            LBM_TRY(count_chunks(g[i], 2, st, &b));
+            cy += a;
+            cz += b;
+        }
+        S->ra = cy < cz ? 1 : 2;
+    }
     std::vector<std::unique_ptr<InstBuild>> builds;
     std::vector<ZSlot> zall;
     int64_t node_off = 0, nch = 0;
     S->inst_off.push_back(0);
     for (size_t i = 0; i < n; ++i) {
         builds.emplace_back(new InstBuild());
-        LBM_TRY(build_instance(g[i], &p[i], (int32_t)i, node_off, (int64_t)zall.size(), st, *builds.back()));
+        LBM_TRY(build_instance(g[i], &p[i], (int32_t)i, S->ra, node_off, (int64_t)zall.size(), st, *builds.back()));
         node_off += builds.back()->N;
         nch += builds.back()->nchunks;
         zall.insert(zall.end(), builds.back()->zslots.begin(), builds.back()->zslots.end());
@@ -502,12 +630,16 @@ lbm_status sim_create(const lbm_geometry* const* g, const lbm_sim_params* p, siz
     // concatenate per-instance arrays
     LBM_CUDA(cudaMalloc(&S->chunks, sizeof(Chunk) * std::max<int64_t>(nch, 1)));
     LBM_CUDA(cudaMalloc(&S->node_grid, sizeof(int64_t) * S->N));
+    if (S->ra != 2) LBM_CUDA(cudaMalloc(&S->out_pos, sizeof(int32_t) * S->N));
     int64_t co = 0;
     for (size_t i = 0; i < n; ++i) {
         LBM_CUDA(cudaMemcpyAsync(S->chunks + co, builds[i]->chunks.p, sizeof(Chunk) * builds[i]->nchunks,
                                  cudaMemcpyDeviceToDevice, st));
         LBM_CUDA(cudaMemcpyAsync(S->node_grid + S->inst_off[i], builds[i]->node_grid.p, sizeof(int64_t) * builds[i]->N,
                                  cudaMemcpyDeviceToDevice, st));
+        if (S->ra != 2)
+            LBM_CUDA(cudaMemcpyAsync(S->out_pos + S->inst_off[i], builds[i]->out_pos.p, sizeof(int32_t) * builds[i]->N,
+                                     cudaMemcpyDeviceToDevice, st));
         co += builds[i]->nchunks;
     }
     LBM_CUDA(cudaMalloc(&S->zslots, sizeof(ZSlot) * std::max<size_t>(zall.size(), 1)));
@@ -683,6 +815,7 @@ lbm_status lbm_sim_info_get(const lbm_sim* S, lbm_sim_info* info) {
     info->precision = S->store;
     info->pattern = S->pattern;
     info->warps_per_block = S->wpb;
+    info->run_axis = S->ra;
     info->state_bytes = (int64_t)S->stride * S->Q * store_bytes(S->store) * (S->pattern == LBM_PULL ? 2 : 1);
     info->algorithmic_bytes_per_update = 2.0 * S->Q * store_bytes(S->store);
     return LBM_OK;
@@ -741,6 +874,7 @@ void lbm_sim_destroy(lbm_sim* S) {
     if (S->insts) cudaFree(S->insts);
     if (S->amp) cudaFree(S->amp);
     if (S->node_grid) cudaFree(S->node_grid);
+    if (S->out_pos) cudaFree(S->out_pos);
     if (S->part) cudaFree(S->part);
     if (S->partbad) cudaFree(S->partbad);
     if (S->mon) cudaFree(S->mon);

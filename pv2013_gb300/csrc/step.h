@@ -1,4 +1,6 @@
-// Launchers of the step kernel instantiations (internal).
+// Launchers of the step kernel instantiations (internal).  One translation
+// unit per storage format so they compile in parallel; the FP64 one is built
+// with -fmad=false.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -9,11 +11,13 @@ namespace lbm {
 
 struct Partials;
 
-// FP64 store (step_f64.cu, built without FMA contraction).
-lbm_status launch_step_f64(int Q, int mode, bool dry, const StepArgs& a, const Partials& p, int warps_per_block,
+lbm_status launch_step_f64(int Q, int mode, bool dry, int ra, const StepArgs& a, const Partials& p, int wpb,
                            cudaStream_t st);
-// FP32 / FP16-shifted / BF16-shifted stores (step_lp.cu).
-lbm_status launch_step_lp(int Q, int store, int mode, bool dry, const StepArgs& a, const Partials& p,
-                          int warps_per_block, cudaStream_t st);
+lbm_status launch_step_f32(int Q, int mode, bool dry, int ra, const StepArgs& a, const Partials& p, int wpb,
+                           cudaStream_t st);
+lbm_status launch_step_f16s(int Q, int mode, bool dry, int ra, const StepArgs& a, const Partials& p, int wpb,
+                            cudaStream_t st);
+lbm_status launch_step_bf16s(int Q, int mode, bool dry, int ra, const StepArgs& a, const Partials& p, int wpb,
+                             cudaStream_t st);
 
 }  // namespace lbm

@@ -24,11 +24,17 @@
 // DRY launches run the gather and boundary part only and write f_n, rho_n,
 // u_n in FP64 (snapshots and monitors); they never modify the state.
 //
+// Neighbour addressing: each lane builds, once, a table over the eight
+// neighbouring columns (node id of its same-level neighbour and the fluid
+// bits one below/at/above), so a population's source or destination costs two
+// integer operations; the chunk's own column is a run and needs none.
+//
 // Arithmetic: Store ST_F64 follows the reference's FP64 expressions operation
 // by operation (its TU is built with -fmad=false), so FP64 runs are bit-exact
-// with the reference.  The other stores compute in FP32 on shifted
-// populations f - w (rho - 1 and f_eq - w formed directly), which keeps the
-// small deviations representable.
+// with the reference.  The other stores compute in FP32 on shifted populations
+// f - w, scaled by 2^15 for FP16 (the scale is folded into the equilibrium,
+// never applied per population), with the equilibrium evaluated for
+// opposite pairs from a symmetric and an antisymmetric part.
 #pragma once
 #include "device.cuh"
 
@@ -36,14 +42,28 @@ namespace lbm {
 
 enum StepMode { MODE_PULL = 0, MODE_AA_EVEN = 1, MODE_AA_ODD = 2 };
 
-template <int S> struct Work { using T = float; };
-template <> struct Work<ST_F64> { using T = double; };
+template <int S> struct Work { using T = float; static constexpr float K = 1.0f; };
+template <> struct Work<ST_F64> { using T = double; static constexpr double K = 1.0; };
+template <> struct Work<ST_F16S> { using T = float; static constexpr float K = kF16Scale; };
 
-// storage -> working value (unshifted for F64, shifted otherwise)
+// Velocity components in (a, b, run) order for a run axis.
+template <int Q, int RA> struct Ax;
+template <int Q> struct Ax<Q, 2> {   // run axis z: columns (x, y)
+    __host__ __device__ static constexpr int a(int q) { return Lat<Q>::cx(q); }
+    __host__ __device__ static constexpr int b(int q) { return Lat<Q>::cy(q); }
+    __host__ __device__ static constexpr int r(int q) { return Lat<Q>::cz(q); }
+};
+template <int Q> struct Ax<Q, 1> {   // run axis y: columns (x, z)
+    __host__ __device__ static constexpr int a(int q) { return Lat<Q>::cx(q); }
+    __host__ __device__ static constexpr int b(int q) { return Lat<Q>::cz(q); }
+    __host__ __device__ static constexpr int r(int q) { return Lat<Q>::cy(q); }
+};
+
+// storage -> working value (F64: f; F32/BF16: f - w; F16: (f - w) * 2^15)
 // (the read-only path is used for the pull pattern only: in the AA patterns
 // the kernel writes the array it reads)
 template <int S, int Q, bool RO = false>
-__device__ __forceinline__ typename Work<S>::T ld(const void* base, int64_t stride, int q, int64_t i) {
+__device__ __forceinline__ typename Work<S>::T ld(const void* base, int64_t stride, int q, int32_t i) {
     if constexpr (S == ST_F64) {
         const double* p = (const double*)base + q * stride + i;
         return RO ? __ldg(p) : *p;
@@ -51,36 +71,38 @@ __device__ __forceinline__ typename Work<S>::T ld(const void* base, int64_t stri
         const float* p = (const float*)base + q * stride + i;
         return (RO ? __ldg(p) : *p) - (float)Lat<Q>::w(q);
     } else if constexpr (S == ST_F16S) {
-        const __half h = ((const __half*)base)[q * stride + i];
-        return __half2float(h) * (1.0f / kF16Scale);
+        const __half* p = (const __half*)base + q * stride + i;
+        return __half2float(RO ? __ldg(p) : *p);
     } else {
-        const __nv_bfloat16 h = ((const __nv_bfloat16*)base)[q * stride + i];
-        return __bfloat162float(h);
+        const __nv_bfloat16* p = (const __nv_bfloat16*)base + q * stride + i;
+        return __bfloat162float(RO ? __ldg(p) : *p);
     }
 }
 
 template <int S, int Q>
-__device__ __forceinline__ void st(void* base, int64_t stride, int q, int64_t i, typename Work<S>::T v) {
+__device__ __forceinline__ void st(void* base, int64_t stride, int q, int32_t i, typename Work<S>::T v) {
     if constexpr (S == ST_F64) {
         ((double*)base)[q * stride + i] = v;
     } else if constexpr (S == ST_F32) {
         ((float*)base)[q * stride + i] = v + (float)Lat<Q>::w(q);
     } else if constexpr (S == ST_F16S) {
-        ((__half*)base)[q * stride + i] = __float2half_rn(v * kF16Scale);
+        ((__half*)base)[q * stride + i] = __float2half_rn(v);
     } else {
         ((__nv_bfloat16*)base)[q * stride + i] = __float2bfloat16_rn(v);
     }
 }
 
-// plain (unshifted) value of a working value
+// working value <-> plain population
 template <int S, int Q>
 __device__ __forceinline__ typename Work<S>::T plain(typename Work<S>::T v, int q) {
     if constexpr (S == ST_F64) return v;
+    else if constexpr (S == ST_F16S) return (float)Lat<Q>::w(q) + v * (1.0f / kF16Scale);
     else return v + (float)Lat<Q>::w(q);
 }
 template <int S, int Q>
 __device__ __forceinline__ typename Work<S>::T unplain(typename Work<S>::T v, int q) {
     if constexpr (S == ST_F64) return v;
+    else if constexpr (S == ST_F16S) return (v - (float)Lat<Q>::w(q)) * kF16Scale;
     else return v - (float)Lat<Q>::w(q);
 }
 
@@ -190,7 +212,8 @@ __device__ __forceinline__ void macro_ref(const T* f, T& rho, T& ux, T& uy, T& u
     }
 }
 
-// BGK collision.  F64: the reference's expressions.  FP32: shifted form.
+// BGK collision.  F64: the reference's expressions.  FP32: shifted (and for
+// FP16 scaled) form with pairwise equilibrium.
 template <int Q, int S>
 __device__ __forceinline__ void collide(typename Work<S>::T* f, const InstParam& ip) {
     using L = Lat<Q>;
@@ -206,6 +229,7 @@ __device__ __forceinline__ void collide(typename Work<S>::T* f, const InstParam&
             f[q] = om * feq + (1.0 - om) * f[q];
         }
     } else {
+        constexpr float K = Work<S>::K;
         float drho = 0.f, jx = 0.f, jy = 0.f, jz = 0.f;
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
@@ -214,32 +238,46 @@ __device__ __forceinline__ void collide(typename Work<S>::T* f, const InstParam&
             if (L::cy(q)) jy += L::cy(q) > 0 ? f[q] : -f[q];
             if (L::cz(q)) jz += L::cz(q) > 0 ? f[q] : -f[q];
         }
-        const float rho = 1.0f + drho;
-        const float inv = 1.0f / rho;
+        const float Krho = K + drho;            // K * rho
+        const float inv = 1.0f / Krho;
         const float ux = jx * inv, uy = jy * inv, uz = jz * inv;
         const float usq15 = 1.5f * (ux * ux + uy * uy + uz * uz);
         const float om = ip.omega_f;
+        const float base = drho - Krho * usq15;    // K (rho - 1) + K rho (-1.5 u^2)
+        const float Krho45 = 4.5f * Krho;
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
-            float cu = 0.f;
-            if (L::cx(q)) cu += L::cx(q) > 0 ? ux : -ux;
-            if (L::cy(q)) cu += L::cy(q) > 0 ? uy : -uy;
-            if (L::cz(q)) cu += L::cz(q) > 0 ? uz : -uz;
-            const float feqs = (float)L::w(q) * (drho + rho * (cu * (3.0f + 4.5f * cu) - usq15));
-            f[q] = f[q] + om * (feqs - f[q]);
+            const int o = L::opp(q);
+            if (o == q) {
+                f[q] += om * ((float)L::w(q) * base - f[q]);
+            } else if (q < o) {
+                float cu = 0.f;
+                if (L::cx(q)) cu += L::cx(q) > 0 ? ux : -ux;
+                if (L::cy(q)) cu += L::cy(q) > 0 ? uy : -uy;
+                if (L::cz(q)) cu += L::cz(q) > 0 ? uz : -uz;
+                const float w = (float)L::w(q);
+                const float sym = w * (base + Krho45 * cu * cu);
+                const float anti = (3.0f * w) * Krho * cu;
+                f[q] += om * ((sym + anti) - f[q]);
+                f[o] += om * ((sym - anti) - f[o]);
+            }
         }
     }
 }
 
-// Source (x - c_q) of population q for lane t of a chunk: node id, or -1.
-template <int Q>
-__device__ __forceinline__ int64_t src_index(const int32_t* base, const uint64_t* mask, int lane, int q) {
-    using L = Lat<Q>;
-    const int d = (1 - L::cx(q)) * 3 + (1 - L::cy(q));
-    const int b = lane - L::cz(q) + 1;
-    const uint64_t m = mask[d];
-    if (!((m >> b) & 1ull)) return -1;
-    return (int64_t)base[d] + __popcll(m & ((1ull << b) - 1ull));
+// Neighbour of a lane at column offset (da, db) and run offset o: existence
+// and node id, from the per-lane table (pb = base + popcount below the lane's
+// own level, bits = fluid at levels -1, 0, +1).
+__device__ __forceinline__ void nbr(const int32_t* pb, const uint32_t* bits, uint32_t own, int32_t n, int da, int db,
+                                    int o, bool& has, int32_t& idx) {
+    if (da == 0 && db == 0) {
+        has = (own >> (1 + o)) & 1u;
+        idx = n + o;
+    } else {
+        const int c = col8(da, db);
+        has = (bits[c] >> (1 + o)) & 1u;
+        idx = pb[c] + (o < 0 ? -(int32_t)(bits[c] & 1u) : (o > 0 ? (int32_t)((bits[c] >> 1) & 1u) : 0));
+    }
 }
 
 struct Partials {
@@ -250,9 +288,10 @@ struct Partials {
     int32_t* bad;
 };
 
-template <int Q, int S, int MODE, bool DRY>
-__global__ void __launch_bounds__(512) k_step(StepArgs a, Partials part) {
+template <int Q, int S, int MODE, bool DRY, int RA>
+__global__ void __launch_bounds__(256) k_step(StepArgs a, Partials part) {
     using L = Lat<Q>;
+    using X = Ax<Q, RA>;
     using T = typename Work<S>::T;
     const int lane = threadIdx.x & 31;
     const int64_t ci = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
@@ -262,28 +301,41 @@ __global__ void __launch_bounds__(512) k_step(StepArgs a, Partials part) {
         const Chunk* cp = a.chunks + ci;
         const int32_t n0 = __ldg(&cp->n0);
         const uint32_t li = __ldg(&cp->len_inst);
-        const uint32_t wmask = __ldg(&cp->wmask), zmask = __ldg(&cp->zmask);
-        int32_t base[9];
-        uint64_t mask[9];
-#pragma unroll
-        for (int d = 0; d < 9; ++d) { base[d] = __ldg(&cp->base[d]); mask[d] = __ldg(&cp->mask[d]); }
-        const int len = (int)(li & 0xffu);
-        const int inst = (int)(li >> 8);
+        const int len = (int)(li & 63u);
         if (lane < len) {
-            const int64_t n = (int64_t)n0 + lane;
+            const uint32_t wmask = __ldg(&cp->wmask), zmask = __ldg(&cp->zmask), bmask = __ldg(&cp->bmask);
+            const int inst = (int)(li >> 8);
+            const int32_t n = n0 + lane;
+            const bool isb = (bmask >> lane) & 1u;
+            const bool tab = MODE != MODE_AA_EVEN || isb;
+            int32_t pb[8];
+            uint32_t bits[8];
+            if (tab) {
+                const uint64_t lm = (2ull << lane) - 1ull;
+#pragma unroll
+                for (int c = 0; c < 8; ++c) {
+                    const uint64_t m = __ldg(&cp->mask[c]);
+                    bits[c] = (uint32_t)(m >> lane) & 7u;
+                    pb[c] = __ldg(&cp->base[c]) + __popcll(m & lm);
+                }
+            }
+            const uint32_t own = ((lane > 0 || ((li >> 6) & 1u)) ? 1u : 0u) | 2u |
+                                 ((lane < len - 1 || ((li >> 7) & 1u)) ? 4u : 0u);
             T f[Q];
             uint32_t missing = 0;
             const void* A = a.src;
 #pragma unroll
             for (int q = 0; q < Q; ++q) {
-                const int64_t s = src_index<Q>(base, mask, lane, q);
-                if (s < 0) missing |= 1u << q;
+                bool has = true;
+                int32_t s = n;
+                if (tab) nbr(pb, bits, own, n, -X::a(q), -X::b(q), -X::r(q), has, s);
+                if (!has) missing |= 1u << q;
                 if constexpr (MODE == MODE_PULL) {
-                    f[q] = s >= 0 ? ld<S, Q, true>(A, a.stride, q, s) : T(0);
+                    f[q] = has ? ld<S, Q, true>(A, a.stride, q, s) : T(0);
                 } else if constexpr (MODE == MODE_AA_EVEN) {
                     f[q] = ld<S, Q>(A, a.stride, q, n);
                 } else {
-                    f[q] = s >= 0 ? ld<S, Q>(A, a.stride, L::opp(q), s) : T(0);
+                    f[q] = has ? ld<S, Q>(A, a.stride, L::opp(q), s) : T(0);
                 }
             }
             if (missing) {
@@ -305,13 +357,11 @@ __global__ void __launch_bounds__(512) k_step(StepArgs a, Partials part) {
             // state, which the reference collides before any boundary condition
             const int64_t step = a.step + (a.step_base ? *a.step_base : 0);
             const bool zl = ((zmask >> lane) & 1u) && step > 0;
-            int zkind = 0;
             double zdir = 0.0;
             if (zl) {
                 const int slot = __ldg(&cp->zslot0) + __popc(zmask & ((1u << lane) - 1u));
                 const ZSlot z = a.zslots[slot];
                 const ListParam lp = a.lists[z.list];
-                zkind = z.kind;
                 T p[Q];
 #pragma unroll
                 for (int q = 0; q < Q; ++q) p[q] = plain<S, Q>(f[q], q);
@@ -338,12 +388,13 @@ __global__ void __launch_bounds__(512) k_step(StepArgs a, Partials part) {
                 for (int q = 0; q < Q; ++q) fp[q] = (double)plain<S, Q>(f[q], q);
                 double rho, ux, uy, uz;
                 macro_ref<Q, double>(fp, rho, ux, uy, uz);
+                const int64_t pos = a.out_pos ? (int64_t)a.out_pos[n] : (int64_t)n;
                 if (a.out_f) {
 #pragma unroll
-                    for (int q = 0; q < Q; ++q) a.out_f[n * Q + q] = fp[q];
+                    for (int q = 0; q < Q; ++q) a.out_f[pos * Q + q] = fp[q];
                 }
-                if (a.out_rho) a.out_rho[n] = rho;
-                if (a.out_u) { a.out_u[3 * n] = ux; a.out_u[3 * n + 1] = uy; a.out_u[3 * n + 2] = uz; }
+                if (a.out_rho) a.out_rho[pos] = rho;
+                if (a.out_u) { a.out_u[3 * pos] = ux; a.out_u[3 * pos + 1] = uy; a.out_u[3 * pos + 2] = uz; }
                 const double sp = sqrt(ux * ux + uy * uy + uz * uz);
                 m_mass = rho;
                 m_maxu = sp;
@@ -352,7 +403,6 @@ __global__ void __launch_bounds__(512) k_step(StepArgs a, Partials part) {
                     if (zdir > 0) m_in = rho * sp;
                     else m_out = rho * sp;
                 }
-                (void)zkind;
             } else {
                 collide<Q, S>(f, a.insts[inst]);
                 void* D = a.dst;
@@ -363,12 +413,11 @@ __global__ void __launch_bounds__(512) k_step(StepArgs a, Partials part) {
                     } else if constexpr (MODE == MODE_AA_EVEN) {
                         st<S, Q>(D, a.stride, L::opp(q), n, f[q]);
                     } else {
-                        if ((missing >> L::opp(q)) & 1u) {
-                            st<S, Q>(D, a.stride, L::opp(q), n, f[q]);
-                        } else {
-                            const int64_t d = src_index<Q>(base, mask, lane, L::opp(q));
-                            st<S, Q>(D, a.stride, q, d, f[q]);
-                        }
+                        bool has;
+                        int32_t d;
+                        nbr(pb, bits, own, n, X::a(q), X::b(q), X::r(q), has, d);
+                        if (has) st<S, Q>(D, a.stride, q, d, f[q]);
+                        else st<S, Q>(D, a.stride, L::opp(q), n, f[q]);
                     }
                 }
             }
@@ -376,9 +425,9 @@ __global__ void __launch_bounds__(512) k_step(StepArgs a, Partials part) {
     }
     if constexpr (DRY) {
         if (part.mass) {
-            // deterministic block reduction: warp shuffles then warp 0
-            __shared__ double sm[4][16];
-            __shared__ int sb[16];
+            // deterministic block reduction: warp shuffles then thread 0
+            __shared__ double sm[4][8];
+            __shared__ int sb[8];
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 m_mass += __shfl_down_sync(0xffffffffu, m_mass, o);

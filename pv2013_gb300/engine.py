@@ -261,7 +261,7 @@ PRECISIONS = {"f64": _capi.F64, "f32": _capi.F32, "f16s": _capi.F16S, "bf16s": _
 PATTERNS = {"pull": _capi.PULL, "aa": _capi.AA, "auto": _capi.AUTO}
 
 
-def _params(Q, precision, pattern, tau, bcs, warps_per_block):
+def _params(Q, precision, pattern, tau, bcs, warps_per_block, run_axis=0):
     cb = [b.to_c() for b in bcs]
     arr = (_capi.ListBC * max(len(cb), 1))(*cb)
     p = _capi.SimParams()
@@ -272,6 +272,7 @@ def _params(Q, precision, pattern, tau, bcs, warps_per_block):
     p.bcs = C.cast(arr, C.POINTER(_capi.ListBC))
     p.nbcs = len(cb)
     p.warps_per_block = int(warps_per_block)
+    p.run_axis = int(run_axis)
     return p, arr
 
 
@@ -282,7 +283,8 @@ class Simulation:
     ``tau`` and ``bcs`` may be per-instance lists).
     """
 
-    def __init__(self, geometry, tau, bcs=(), Q=19, precision="f64", pattern="pull", warps_per_block=0, stream=None):
+    def __init__(self, geometry, tau, bcs=(), Q=19, precision="f64", pattern="pull", warps_per_block=0, run_axis=0,
+                 stream=None):
         lib = load()
         self._stream = C.c_void_p(stream) if stream else None
         h = C.c_void_p()
@@ -293,14 +295,14 @@ class Simulation:
             keep = []
             params = (_capi.SimParams * n)()
             for i in range(n):
-                p, arr = _params(Q, precision, pattern, taus[i], bcl[i], warps_per_block)
+                p, arr = _params(Q, precision, pattern, taus[i], bcl[i], warps_per_block, run_axis)
                 keep.append((arr, bcl[i]))
                 params[i] = p
             geoms = (C.c_void_p * n)(*[g.handle for g in geometry])
             check(lib.lbm_batch_create(geoms, params, n, self._stream, C.byref(h)))
             self.geometries = list(geometry)
         else:
-            p, arr = _params(Q, precision, pattern, tau, bcs, warps_per_block)
+            p, arr = _params(Q, precision, pattern, tau, bcs, warps_per_block, run_axis)
             check(lib.lbm_sim_create(geometry.handle, C.byref(p), self._stream, C.byref(h)))
             self.geometries = [geometry]
         self._h = h

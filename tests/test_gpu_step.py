@@ -23,13 +23,17 @@ def rel_l2(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
+@pytest.mark.parametrize("run_axis", [1, 2])
 @pytest.mark.parametrize("pattern", ["pull", "aa"])
 @pytest.mark.parametrize("steps", [1, 2, 37])
-def test_fp64_pipe_bit_exact(oracle_mod, pattern, steps):
+def test_fp64_pipe_bit_exact(oracle_mod, pattern, steps, run_axis):
+    """Both node numberings (runs along y or along z) give the reference's
+    populations; outputs are in the reference's x-major node order."""
     O = oracle_mod
     c = cases.pipe()
     geom = c.geometry()
-    sim = Simulation(geom, c.tau, c.boundary_specs(geom), precision="f64", pattern=pattern)
+    sim = Simulation(geom, c.tau, c.boundary_specs(geom), precision="f64", pattern=pattern, run_axis=run_axis)
+    assert sim.info().run_axis == run_axis
     sim.step(steps)
     f, rho, u = sim.fields()
     _, ref = oracle_run(O, c, geom, steps)
@@ -53,13 +57,13 @@ def test_fp64_graph_replay_equals_direct(pattern):
     assert np.array_equal(a.fields()[0], b.fields()[0])
 
 
-@pytest.mark.parametrize("pattern", ["pull", "aa"])
-def test_fp64_pulsatile_vessel_bit_exact(oracle_mod, pattern):
+@pytest.mark.parametrize("pattern,run_axis", [("pull", 2), ("aa", 1), ("aa", 0)])
+def test_fp64_pulsatile_vessel_bit_exact(oracle_mod, pattern, run_axis):
     O = oracle_mod
     c = cases.vessel(4001)
     c.inlet.period = 9
     geom = c.geometry()
-    sim = Simulation(geom, c.tau, c.boundary_specs(geom), precision="f64", pattern=pattern)
+    sim = Simulation(geom, c.tau, c.boundary_specs(geom), precision="f64", pattern=pattern, run_axis=run_axis)
     sim.step(25)
     _, ref = oracle_run(O, c, geom, 25)
     assert np.array_equal(sim.fields()[0], ref.f())
@@ -105,7 +109,7 @@ def test_batch_equals_individual_runs():
     c1, c2 = cases.pipe(), cases.vessel(4002)
     g1, g2 = c1.geometry(), c2.geometry()
     batch = Simulation([g1, g2], [c1.tau, c2.tau], [c1.boundary_specs(g1), c2.boundary_specs(g2)],
-                       precision="f64", pattern="aa")
+                       precision="f64", pattern="aa", run_axis=1)
     s1 = Simulation(g1, c1.tau, c1.boundary_specs(g1), precision="f64", pattern="aa")
     s2 = Simulation(g2, c2.tau, c2.boundary_specs(g2), precision="f64", pattern="aa")
     for s in (batch, s1, s2):
@@ -114,17 +118,20 @@ def test_batch_equals_individual_runs():
     fb = batch.fields()[0]
     assert np.array_equal(fb[off[0]:off[1]], s1.fields()[0])
     assert np.array_equal(fb[off[1]:off[2]], s2.fields()[0])
+    nodes = batch.nodes()
+    assert np.array_equal(nodes[off[0]:off[1]], s1.nodes()) and np.array_equal(nodes[off[1]:off[2]], s2.nodes())
 
 
 @pytest.mark.parametrize("precision,pattern,tol", [("f32", "pull", 2e-5), ("f32", "aa", 2e-5),
                                                     ("f16s", "aa", 1e-3), ("f16s", "pull", 1e-3),
                                                     ("bf16s", "aa", 3e-2)])
-def test_reduced_precision_velocity_error(oracle_mod, precision, pattern, tol):
+@pytest.mark.parametrize("run_axis", [1, 2])
+def test_reduced_precision_velocity_error(oracle_mod, precision, pattern, tol, run_axis):
     """Velocity relative L2 error vs the FP64 oracle after 400 steps of the pipe."""
     O = oracle_mod
     c = cases.pipe()
     geom = c.geometry()
-    sim = Simulation(geom, c.tau, c.boundary_specs(geom), precision=precision, pattern=pattern)
+    sim = Simulation(geom, c.tau, c.boundary_specs(geom), precision=precision, pattern=pattern, run_axis=run_axis)
     sim.step(400)
     _, rho, u = sim.fields()
     _, ref = oracle_run(O, c, geom, 400)
