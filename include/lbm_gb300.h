@@ -202,6 +202,7 @@ typedef struct lbm_sim_params {
     int32_t run_axis;          /* node numbering axis (chunks are runs along it):
                                   1 = y, 2 = z (the reference's x-major order),
                                   0 = the one giving fewer chunks */
+    int32_t staging;           /* 0 = TMA-staged pipeline (default), 1 = direct loads */
 } lbm_sim_params;
 
 typedef struct lbm_sim lbm_sim;

@@ -63,7 +63,7 @@ class ListBC(C.Structure):
 class SimParams(C.Structure):
     _fields_ = [("Q", C.c_int32), ("precision", C.c_int32), ("pattern", C.c_int32), ("tau", C.c_double),
                 ("bcs", C.POINTER(ListBC)), ("nbcs", C.c_size_t), ("warps_per_block", C.c_int32),
-                ("run_axis", C.c_int32)]
+                ("run_axis", C.c_int32), ("staging", C.c_int32)]
 
 
 class SimInfo(C.Structure):

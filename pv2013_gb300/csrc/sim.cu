@@ -309,7 +309,8 @@ int store_bytes(int s) { return s == ST_F64 ? 8 : (s == ST_F32 ? 4 : 2); }
 
 struct lbm_sim {
     int dev = 0;
-    int Q = 19, store = ST_F64, pattern = LBM_PULL, wpb = 4, ra = 2;
+    int Q = 19, store = ST_F64, pattern = LBM_PULL, wpb = 4, ra = 2, staging = 0;
+    int32_t* err = nullptr;        // device flag: a bounded wait in the step kernel gave up
     int64_t N = 0, nchunks = 0, stride = 0, nz = 0;
     int64_t n_inst = 0;
     void* buf[2] = {nullptr, nullptr};
@@ -513,6 +514,14 @@ lbm_status sim_launch(lbm_sim* S, int mode, bool dry, void* src, void* dst, int6
     a.zslots = S->zslots; a.lists = S->lists; a.insts = S->insts; a.amp = S->amp;
     a.step = step; a.step_base = step_base;
     a.out_f = of; a.out_rho = orho; a.out_u = ou; a.out_pos = S->out_pos; a.n_nodes = S->N;
+    if (!dry && S->staging == 0) {
+        switch (S->store) {
+            case ST_F64: return launch_tma_f64(S->Q, mode, S->ra, a, S->err, S->wpb, st);
+            case ST_F32: return launch_tma_f32(S->Q, mode, S->ra, a, S->err, S->wpb, st);
+            case ST_F16S: return launch_tma_f16s(S->Q, mode, S->ra, a, S->err, S->wpb, st);
+            default: return launch_tma_bf16s(S->Q, mode, S->ra, a, S->err, S->wpb, st);
+        }
+    }
     switch (S->store) {
         case ST_F64: return launch_step_f64(S->Q, mode, dry, S->ra, a, part, S->wpb, st);
         case ST_F32: return launch_step_f32(S->Q, mode, dry, S->ra, a, part, S->wpb, st);
@@ -557,7 +566,17 @@ lbm_status sim_dry(lbm_sim* S, double* of, double* orho, double* ou, bool partia
     return LBM_OK;
 }
 
+// Reads the step kernel's error flag (synchronises the stream).
+lbm_status check_timeout(lbm_sim* S, cudaStream_t st) {
+    int32_t e = 0;
+    LBM_CUDA(cudaMemcpyAsync(&e, S->err, sizeof e, cudaMemcpyDeviceToHost, st));
+    LBM_CUDA(cudaStreamSynchronize(st));
+    if (e) return fail(LBM_ERR_TIMEOUT, "a bounded wait in the step kernel gave up (staged copies did not arrive)");
+    return LBM_OK;
+}
+
 lbm_status sim_monitors(lbm_sim* S, lbm_monitors* out, cudaStream_t st) {
+    LBM_TRY(check_timeout(S, st));
     LBM_TRY(sim_dry(S, nullptr, nullptr, nullptr, true, st));
     MonOut h;
     LBM_CUDA(cudaMemcpyAsync(&h, S->mon, sizeof h, cudaMemcpyDeviceToHost, st));
@@ -592,6 +611,8 @@ lbm_status sim_create(const lbm_geometry* const* g, const lbm_sim_params* p, siz
     S->wpb = p0.warps_per_block > 0 ? p0.warps_per_block : 4;
     if (S->wpb > 8) return fail(LBM_ERR_ARG, "warps_per_block must be <= 8");
     if (p0.run_axis != 0 && p0.run_axis != 1 && p0.run_axis != 2) return fail(LBM_ERR_ARG, "run_axis must be 0, 1 or 2");
+    if (p0.staging != 0 && p0.staging != 1) return fail(LBM_ERR_ARG, "staging must be 0 or 1");
+    S->staging = p0.staging;
     for (size_t i = 0; i < n; ++i) {
         if (p[i].Q != p0.Q || p[i].precision != p0.precision || p[i].pattern != p0.pattern)
             return fail(LBM_ERR_ARG, "batch members must share Q, precision and pattern");
@@ -710,6 +731,8 @@ lbm_status sim_create(const lbm_geometry* const* g, const lbm_sim_params* p, siz
     LBM_CUDA(cudaMalloc(&S->partbad, sizeof(int32_t) * S->part_blocks));
     LBM_CUDA(cudaMalloc(&S->mon, sizeof(MonOut)));
     LBM_CUDA(cudaMalloc(&S->step_base, sizeof(int64_t)));
+    LBM_CUDA(cudaMalloc(&S->err, sizeof(int32_t)));
+    LBM_CUDA(cudaMemsetAsync(S->err, 0, sizeof(int32_t), st));
     LBM_CUDA(cudaGetLastError());
     LBM_CUDA(cudaStreamSynchronize(st));
     lbm_monitors m;
@@ -830,6 +853,7 @@ lbm_status lbm_sim_fields(lbm_sim* S, double* rho, double* u, double* f, size_t 
     if (f) LBM_TRY(df.alloc((size_t)S->N * S->Q, "field f"));
     if (rho) LBM_TRY(dr.alloc(S->N, "field rho"));
     if (u) LBM_TRY(du.alloc((size_t)S->N * 3, "field u"));
+    LBM_TRY(check_timeout(S, st));
     LBM_TRY(sim_dry(S, df.p, dr.p, du.p, false, st));
     if (f) LBM_CUDA(cudaMemcpyAsync(f, df.p, sizeof(double) * S->N * S->Q, cudaMemcpyDeviceToHost, st));
     if (rho) LBM_CUDA(cudaMemcpyAsync(rho, dr.p, sizeof(double) * S->N, cudaMemcpyDeviceToHost, st));
@@ -879,6 +903,7 @@ void lbm_sim_destroy(lbm_sim* S) {
     if (S->partbad) cudaFree(S->partbad);
     if (S->mon) cudaFree(S->mon);
     if (S->step_base) cudaFree(S->step_base);
+    if (S->err) cudaFree(S->err);
     delete S;
 }
 

@@ -20,4 +20,10 @@ lbm_status launch_step_f16s(int Q, int mode, bool dry, int ra, const StepArgs& a
 lbm_status launch_step_bf16s(int Q, int mode, bool dry, int ra, const StepArgs& a, const Partials& p, int wpb,
                              cudaStream_t st);
 
+// TMA-staged pipeline (non-dry launches only); err receives 1 if a bounded wait gave up.
+lbm_status launch_tma_f64(int Q, int mode, int ra, const StepArgs& a, int32_t* err, int wpb, cudaStream_t st);
+lbm_status launch_tma_f32(int Q, int mode, int ra, const StepArgs& a, int32_t* err, int wpb, cudaStream_t st);
+lbm_status launch_tma_f16s(int Q, int mode, int ra, const StepArgs& a, int32_t* err, int wpb, cudaStream_t st);
+lbm_status launch_tma_bf16s(int Q, int mode, int ra, const StepArgs& a, int32_t* err, int wpb, cudaStream_t st);
+
 }  // namespace lbm

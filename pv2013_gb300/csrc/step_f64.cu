@@ -10,4 +10,8 @@ lbm_status launch_step_f64(int Q, int mode, bool dry, int ra, const StepArgs& a,
     return launch_store<ST_F64>(Q, mode, dry, ra, a, p, wpb, st);
 }
 
+lbm_status launch_tma_f64(int Q, int mode, int ra, const StepArgs& a, int32_t* err, int wpb, cudaStream_t st) {
+    return launch_store_tma<ST_F64>(Q, mode, ra, a, err, wpb, st);
+}
+
 }  // namespace lbm

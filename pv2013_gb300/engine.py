@@ -261,7 +261,7 @@ PRECISIONS = {"f64": _capi.F64, "f32": _capi.F32, "f16s": _capi.F16S, "bf16s": _
 PATTERNS = {"pull": _capi.PULL, "aa": _capi.AA, "auto": _capi.AUTO}
 
 
-def _params(Q, precision, pattern, tau, bcs, warps_per_block, run_axis=0):
+def _params(Q, precision, pattern, tau, bcs, warps_per_block, run_axis=0, staging=0):
     cb = [b.to_c() for b in bcs]
     arr = (_capi.ListBC * max(len(cb), 1))(*cb)
     p = _capi.SimParams()
@@ -273,6 +273,7 @@ def _params(Q, precision, pattern, tau, bcs, warps_per_block, run_axis=0):
     p.nbcs = len(cb)
     p.warps_per_block = int(warps_per_block)
     p.run_axis = int(run_axis)
+    p.staging = int(staging)
     return p, arr
 
 
@@ -284,7 +285,7 @@ class Simulation:
     """
 
     def __init__(self, geometry, tau, bcs=(), Q=19, precision="f64", pattern="pull", warps_per_block=0, run_axis=0,
-                 stream=None):
+                 staging=0, stream=None):
         lib = load()
         self._stream = C.c_void_p(stream) if stream else None
         h = C.c_void_p()
@@ -295,14 +296,14 @@ class Simulation:
             keep = []
             params = (_capi.SimParams * n)()
             for i in range(n):
-                p, arr = _params(Q, precision, pattern, taus[i], bcl[i], warps_per_block, run_axis)
+                p, arr = _params(Q, precision, pattern, taus[i], bcl[i], warps_per_block, run_axis, staging)
                 keep.append((arr, bcl[i]))
                 params[i] = p
             geoms = (C.c_void_p * n)(*[g.handle for g in geometry])
             check(lib.lbm_batch_create(geoms, params, n, self._stream, C.byref(h)))
             self.geometries = list(geometry)
         else:
-            p, arr = _params(Q, precision, pattern, tau, bcs, warps_per_block, run_axis)
+            p, arr = _params(Q, precision, pattern, tau, bcs, warps_per_block, run_axis, staging)
             check(lib.lbm_sim_create(geometry.handle, C.byref(p), self._stream, C.byref(h)))
             self.geometries = [geometry]
         self._h = h

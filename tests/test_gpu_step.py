@@ -23,16 +23,19 @@ def rel_l2(a, b):
     return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
 
 
+@pytest.mark.parametrize("staging", [0, 1])
 @pytest.mark.parametrize("run_axis", [1, 2])
 @pytest.mark.parametrize("pattern", ["pull", "aa"])
 @pytest.mark.parametrize("steps", [1, 2, 37])
-def test_fp64_pipe_bit_exact(oracle_mod, pattern, steps, run_axis):
-    """Both node numberings (runs along y or along z) give the reference's
-    populations; outputs are in the reference's x-major node order."""
+def test_fp64_pipe_bit_exact(oracle_mod, pattern, steps, run_axis, staging):
+    """Both node numberings (runs along y or along z) and both kernels (TMA-staged
+    pipeline, direct loads) give the reference's populations; outputs are in the
+    reference's x-major node order."""
     O = oracle_mod
     c = cases.pipe()
     geom = c.geometry()
-    sim = Simulation(geom, c.tau, c.boundary_specs(geom), precision="f64", pattern=pattern, run_axis=run_axis)
+    sim = Simulation(geom, c.tau, c.boundary_specs(geom), precision="f64", pattern=pattern, run_axis=run_axis,
+                     staging=staging)
     assert sim.info().run_axis == run_axis
     sim.step(steps)
     f, rho, u = sim.fields()
@@ -57,13 +60,14 @@ def test_fp64_graph_replay_equals_direct(pattern):
     assert np.array_equal(a.fields()[0], b.fields()[0])
 
 
-@pytest.mark.parametrize("pattern,run_axis", [("pull", 2), ("aa", 1), ("aa", 0)])
-def test_fp64_pulsatile_vessel_bit_exact(oracle_mod, pattern, run_axis):
+@pytest.mark.parametrize("pattern,run_axis,staging", [("pull", 2, 0), ("aa", 1, 0), ("aa", 0, 0), ("pull", 1, 1)])
+def test_fp64_pulsatile_vessel_bit_exact(oracle_mod, pattern, run_axis, staging):
     O = oracle_mod
     c = cases.vessel(4001)
     c.inlet.period = 9
     geom = c.geometry()
-    sim = Simulation(geom, c.tau, c.boundary_specs(geom), precision="f64", pattern=pattern, run_axis=run_axis)
+    sim = Simulation(geom, c.tau, c.boundary_specs(geom), precision="f64", pattern=pattern, run_axis=run_axis,
+                     staging=staging)
     sim.step(25)
     _, ref = oracle_run(O, c, geom, 25)
     assert np.array_equal(sim.fields()[0], ref.f())
