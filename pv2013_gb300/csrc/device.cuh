@@ -68,27 +68,32 @@ template <> struct Lat<27> {
 };
 
 // ---------------------------------------------------------------------------
-// Run-table lattice.  Fluid nodes are numbered with the run axis fastest
-// (z for the reference's x-major order; y when the vessels run along y);
-// each run of consecutive fluid points along that axis is cut into chunks of
-// at most 32 nodes, one warp per chunk.  The two other axes (a, b) span the
-// grid columns.  For the eight neighbouring columns (a+da, b+db) a chunk
-// holds a fluid bit mask over the window r0-1 .. r0+32 along the run axis
-// (bit p <-> r0-1+p) and the node id of the lowest fluid point of that window,
-// so the node id of a neighbour of lane t is base + popcount(mask below its
-// bit).  The chunk's own column is a run: only its two end bits are stored.
-struct __align__(128) Chunk {
-    int32_t n0;        // node id of lane 0
-    uint32_t len_inst; // bits 0-5: nodes (1..32); bit 6: own column fluid at r0-1;
-                       // bit 7: own column fluid at r0+len; bits 8-31: instance
+// Ghost-padded run lattice.  Nodes are the fluid points plus a one-cell ghost
+// layer (points that are not fluid but have a fluid point among their 26
+// neighbours, on a grid padded by one cell so the layer is complete).  Nodes
+// are numbered with the run axis fastest (z in the reference's x-major order,
+// y when the vessels run along y); the two other axes (a, b) span the grid
+// columns.  Each run of consecutive fluid points along the run axis is cut
+// into chunks of at most 32 nodes, one warp per chunk, one lane per node.
+//
+// Because every 26-neighbour of a fluid point is a node, each neighbouring
+// column holds nodes at every level r0-1 .. r0+len of a chunk, with
+// consecutive ids; so the node id of a neighbour of lane t at column offset
+// (da, db) and level offset o is K[col8(da, db)] + 1 + o + t (own column:
+// n0 + o + t).  Ghost nodes are never updated; a boundary node carries a
+// mask of the populations whose source is a ghost ("missing").
+struct __align__(64) Chunk {
+    int32_t n0;        // node id of lane 0 (every lane is a fluid node)
+    uint32_t len_inst; // bits 0-5: nodes (1..32); bits 8-31: instance
     uint32_t wmask;    // lanes that are wall nodes (bounce-back)
     uint32_t zmask;    // lanes that carry a Zou-He boundary condition
-    uint32_t bmask;    // lanes that are boundary nodes (may miss a neighbour)
+    uint32_t bmask;    // lanes that are boundary nodes (may miss a source)
     int32_t zslot0;    // Zou-He slot of the first zmask lane
-    int32_t base[8];   // neighbour columns, index col8(da, db)
-    uint64_t mask[8];
+    int32_t mslot0;    // missing-mask slot of the first bmask lane
+    int32_t K[8];      // neighbour columns: node id at level r0-1, index col8(da, db)
+    int32_t pad;
 };
-static_assert(sizeof(Chunk) == 128, "chunk descriptor is one 128-byte line");
+static_assert(sizeof(Chunk) == 64, "chunk descriptor is one 64-byte sector pair");
 
 // (da, db) in {-1,0,1}^2 minus (0,0) -> 0..7
 __host__ __device__ constexpr int col8(int da, int db) {
@@ -133,6 +138,7 @@ template <> struct StoreT<ST_BF16S> { using T = __nv_bfloat16; static constexpr 
 struct StepArgs {
     const Chunk* chunks;
     int64_t nchunks;
+    const uint32_t* mmask;    // missing-population masks of boundary lanes
     const void* src;          // populations read (pull) / the single lattice (AA)
     void* dst;                // populations written (pull) / same as src (AA)
     int64_t stride;           // elements between population planes (SoA)
@@ -146,7 +152,7 @@ struct StepArgs {
     double* out_f;
     double* out_rho;
     double* out_u;
-    const int32_t* out_pos;   // output position of each node (x-major rank), or null = identity
+    const int32_t* out_pos;   // output position of each node (x-major rank of the fluid point)
     int64_t n_nodes;
 };
 

@@ -106,23 +106,66 @@ __global__ void k_permute_flags(const uint8_t* __restrict__ in, Perm P, uint8_t*
         out[P.to_perm(o)] = in[o];
 }
 
-__global__ void k_to_orig(int64_t* __restrict__ idx, int64_t n, Perm P) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        idx[i] = P.to_orig(idx[i]);
+// Node types on the padded permuted grid (one extra cell on every side):
+// 2 fluid, 1 ghost (not fluid, a fluid point among its 26 neighbours), 0 none.
+struct Pad {
+    int Na, Nb, Nr;                       // unpadded permuted dims
+    __host__ __device__ int64_t Pa() const { return Na + 2; }
+    __host__ __device__ int64_t Pb() const { return Nb + 2; }
+    __host__ __device__ int64_t Pr() const { return Nr + 2; }
+    __host__ __device__ int64_t cells() const { return Pa() * Pb() * Pr(); }
+    __host__ __device__ int64_t cell(int64_t a, int64_t b, int64_t r) const { return (a * Pb() + b) * Pr() + r; }
+};
+
+__global__ void k_types(const uint8_t* __restrict__ pflags, Pad D, uint8_t* __restrict__ type) {
+    const int64_t n = D.cells();
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = c % D.Pr(), t = c / D.Pr();
+        const int64_t b = t % D.Pb(), a = t / D.Pb();
+        auto fluid = [&](int64_t aa, int64_t bb, int64_t rr) {
+            return aa >= 1 && aa <= D.Na && bb >= 1 && bb <= D.Nb && rr >= 1 && rr <= D.Nr &&
+                   pflags[((aa - 1) * D.Nb + (bb - 1)) * D.Nr + (rr - 1)] != 0;
+        };
+        uint8_t ty = 0;
+        if (fluid(a, b, r)) {
+            ty = 2;
+        } else {
+            for (int da = -1; da <= 1 && !ty; ++da)
+                for (int db = -1; db <= 1 && !ty; ++db)
+                    for (int dr = -1; dr <= 1 && !ty; ++dr)
+                        if (fluid(a + da, b + db, r + dr)) ty = 1;
+        }
+        type[c] = ty;
+    }
 }
 
-// out_pos[n] = node_off + x-major rank of node n (rank_of_point holds the rank of each fluid point)
-__global__ void k_xrank(const int64_t* __restrict__ node_orig, int64_t n, const int32_t* __restrict__ rank_of_point,
-                        int64_t node_off, int32_t* __restrict__ pos) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-        pos[i] = (int32_t)(node_off + rank_of_point[node_orig[i]]);
+// out_pos of every node: x-major rank of its fluid point (ghosts: -1)
+__global__ void k_out_pos(const int64_t* __restrict__ node_cell, int64_t n, const uint8_t* __restrict__ type, Pad D,
+                          Perm P, const int32_t* __restrict__ rank_of_point, int64_t out_off, int32_t* __restrict__ pos) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t c = node_cell[i];
+        if (type[c] != 2) { pos[i] = -1; continue; }
+        const int64_t r = c % D.Pr(), t = c / D.Pr();
+        const int64_t b = t % D.Pb(), a = t / D.Pb();
+        const int64_t p = ((a - 1) * D.Nb + (b - 1)) * D.Nr + (r - 1);
+        pos[i] = (int32_t)(out_off + rank_of_point[P.to_orig(p)]);
+    }
 }
 
-// role: 0 interior, 1 wall, 2+l first matching predicate list l
-__global__ void k_roles(const int64_t* __restrict__ bidx, const uint64_t* __restrict__ bmask, int64_t nb, Perm P,
-                        const int32_t* __restrict__ node_of_point, int8_t* __restrict__ role) {
+// role per node: -1 ghost, 0 interior, 1 wall, 2+l first matching predicate list l
+__global__ void k_roles_fluid(const int64_t* __restrict__ node_cell, int64_t n, const uint8_t* __restrict__ type,
+                              int8_t* __restrict__ role) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        role[i] = type[node_cell[i]] == 2 ? 0 : -1;
+}
+
+__global__ void k_roles(const int64_t* __restrict__ bidx, const uint64_t* __restrict__ bmask, int64_t nb, Perm P, Pad D,
+                        const int32_t* __restrict__ node_of_cell, int8_t* __restrict__ role) {
     for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b < nb; b += (int64_t)gridDim.x * blockDim.x) {
-        const int32_t n = node_of_point[P.to_perm(bidx[b])];
+        const int64_t p = P.to_perm(bidx[b]);
+        const int64_t r = p % D.Nr, t = p / D.Nr;
+        const int64_t bb = t % D.Nb, a = t / D.Nb;
+        const int32_t n = node_of_cell[D.cell(a + 1, bb + 1, r + 1)];
         const uint64_t m = bmask[b];
         role[n] = m ? (int8_t)(2 + __ffsll((long long)m) - 1) : (int8_t)1;
     }
@@ -141,36 +184,52 @@ __global__ void k_gather_role(const int64_t* __restrict__ ids, int64_t n, const 
         out[i] = role[ids[i]];
 }
 
-// chunks per grid column (permuted layout, runs along the last axis)
-__global__ void k_col_count(const uint8_t* __restrict__ flags, int Na, int Nb, int Nr, int32_t* __restrict__ cnt) {
-    const int64_t ncol = (int64_t)Na * Nb;
+// per padded column (a, b): chunks (runs of fluid cells, <= 32) and boundary lanes
+__global__ void k_col_count(const uint8_t* __restrict__ type, const int32_t* __restrict__ node_of_cell,
+                            const int8_t* __restrict__ role, Pad D, int32_t* __restrict__ nchunk,
+                            int32_t* __restrict__ nbound) {
+    const int64_t ncol = (int64_t)D.Na * D.Nb;
     for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncol; c += (int64_t)gridDim.x * blockDim.x) {
-        const uint8_t* f = flags + c * Nr;
-        int32_t n = 0;
+        const int64_t a = c / D.Nb + 1, b = c % D.Nb + 1;
+        const int64_t base = D.cell(a, b, 0);
+        int32_t nc = 0, nbd = 0;
         int run = 0;
-        for (int k = 0; k <= Nr; ++k) {
-            const bool fl = k < Nr && f[k];
-            if (fl) ++run;
+        for (int64_t r = 0; r <= D.Pr(); ++r) {
+            const bool fl = r < D.Pr() && type[base + r] == 2;
+            if (fl) {
+                ++run;
+                if (role[node_of_cell[base + r]] >= 1) ++nbd;
+            }
             if (!fl || run == 32) {
-                if (run > 0) ++n;
+                if (run > 0) ++nc;
                 run = 0;
             }
         }
-        cnt[c] = n;
+        nchunk[c] = nc;
+        nbound[c] = nbd;
     }
 }
 
+struct Vel {
+    int8_t a[27], b[27], r[27];   // velocity components in (column a, column b, run) order
+    int Q;
+};
+
 struct FillArgs {
-    const uint8_t* flags;         // permuted layout
-    int Na, Nb, Nr;
-    const int64_t* chunk_off;     // per column
-    const int32_t* node_of_point; // local ids, permuted layout
+    const uint8_t* type;
+    const int32_t* node_of_cell;
     const int8_t* role;
+    Pad D;
+    Vel V;
+    const int64_t* chunk_off;     // per column
+    const int64_t* mslot_off;     // per column
     const int64_t* znodes;        // sorted local ids of Zou-He nodes
     int64_t nz;
-    int64_t node_off, zslot_off;
+    int64_t node_off, zslot_off, mslot_base;
     int32_t inst;
     Chunk* chunks;
+    uint32_t* mmask;
+    int32_t* err;
 };
 
 __device__ int64_t lower_bound_i64(const int64_t* a, int64_t n, int64_t v) {
@@ -183,58 +242,57 @@ __device__ int64_t lower_bound_i64(const int64_t* a, int64_t n, int64_t v) {
 }
 
 __global__ void k_col_fill(FillArgs A) {
-    const int64_t ncol = (int64_t)A.Na * A.Nb;
+    const Pad& D = A.D;
+    const int64_t ncol = (int64_t)D.Na * D.Nb;
     for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncol; c += (int64_t)gridDim.x * blockDim.x) {
-        const int i = (int)(c / A.Nb), j = (int)(c % A.Nb);
-        const uint8_t* f = A.flags + c * A.Nr;
+        const int64_t a = c / D.Nb + 1, b = c % D.Nb + 1;
+        const int64_t base = D.cell(a, b, 0);
         int64_t out = A.chunk_off[c];
-        int run = 0, k0 = 0;
-        for (int k = 0; k <= A.Nr; ++k) {
-            const bool fl = k < A.Nr && f[k];
-            if (fl) { if (run == 0) k0 = k; ++run; }
+        int64_t ms = A.mslot_off[c];
+        int run = 0;
+        int64_t r0 = 0;
+        for (int64_t r = 0; r <= D.Pr(); ++r) {
+            const bool fl = r < D.Pr() && A.type[base + r] == 2;
+            if (fl) { if (run == 0) r0 = r; ++run; }
             if (!fl || run == 32) {
                 if (run > 0) {
                     Chunk ch;
-                    const int32_t n0 = A.node_of_point[c * A.Nr + k0];
-                    const uint32_t e0 = (k0 > 0 && f[k0 - 1]) ? 1u : 0u;
-                    const uint32_t e1 = (k0 + run < A.Nr && f[k0 + run]) ? 1u : 0u;
+                    const int32_t n0 = A.node_of_cell[base + r0];
                     ch.n0 = (int32_t)(A.node_off + n0);
-                    ch.len_inst = (uint32_t)run | (e0 << 6) | (e1 << 7) | ((uint32_t)A.inst << 8);
-                    ch.wmask = 0;
-                    ch.zmask = 0;
-                    ch.bmask = 0;
+                    ch.len_inst = (uint32_t)run | ((uint32_t)A.inst << 8);
+                    ch.wmask = ch.zmask = ch.bmask = 0;
+                    ch.pad = 0;
+                    ch.mslot0 = (int32_t)(A.mslot_base + ms);
                     for (int t = 0; t < run; ++t) {
-                        const int r = A.role[n0 + t];
-                        if (r == 1) ch.wmask |= 1u << t;
-                        if (r >= 1) ch.bmask |= 1u << t;
+                        const int ro = A.role[n0 + t];
+                        if (ro == 1) ch.wmask |= 1u << t;
+                        if (ro >= 1) {
+                            ch.bmask |= 1u << t;
+                            uint32_t m = 0;
+                            for (int q = 0; q < A.V.Q; ++q) {
+                                const int64_t sc = D.cell(a - A.V.a[q], b - A.V.b[q], r0 + t - A.V.r[q]);
+                                if (A.type[sc] != 2) m |= 1u << q;
+                            }
+                            A.mmask[ms++] = m;
+                        }
                     }
                     const int64_t zfirst = lower_bound_i64(A.znodes, A.nz, n0);
                     ch.zslot0 = (int32_t)(A.zslot_off + zfirst);
                     for (int64_t zz = zfirst; zz < A.nz && A.znodes[zz] < n0 + run; ++zz)
                         ch.zmask |= 1u << (int)(A.znodes[zz] - n0);
-                    for (int di = -1; di <= 1; ++di)
-                        for (int dj = -1; dj <= 1; ++dj) {
-                            if (di == 0 && dj == 0) continue;
-                            const int d = col8(di, dj);
-                            const int a = i + di, b = j + dj;
-                            uint64_t m = 0;
-                            int32_t base = 0;
-                            if (a >= 0 && a < A.Na && b >= 0 && b < A.Nb) {
-                                const int64_t cc = (int64_t)a * A.Nb + b;
-                                const uint8_t* g = A.flags + cc * A.Nr;
-                                int first = -1;
-                                for (int bit = 0; bit < 34; ++bit) {
-                                    const int kk = k0 - 1 + bit;
-                                    if (kk >= 0 && kk < A.Nr && g[kk]) {
-                                        m |= 1ull << bit;
-                                        if (first < 0) first = kk;
-                                    }
-                                }
-                                if (first >= 0) base = (int32_t)(A.node_off + A.node_of_point[cc * A.Nr + first]);
-                            }
-                            ch.mask[d] = m;
-                            ch.base[d] = base;
+                    for (int da = -1; da <= 1; ++da)
+                        for (int db = -1; db <= 1; ++db) {
+                            if (da == 0 && db == 0) continue;
+                            const int32_t k = A.node_of_cell[D.cell(a + da, b + db, r0 - 1)];
+                            // every level r0-1 .. r0+run of a neighbour column is a node
+                            // with consecutive ids (ghost layer); checked at both ends
+                            const int32_t k2 = A.node_of_cell[D.cell(a + da, b + db, r0 + run)];
+                            if (k < 0 || k2 != k + run + 1) atomicOr(A.err, 1);
+                            ch.K[col8(da, db)] = (int32_t)(A.node_off + (k < 0 ? 0 : k));
                         }
+                    if (n0 < 1 || A.node_of_cell[base + r0 - 1] != n0 - 1 ||
+                        A.node_of_cell[base + r0 + run] != n0 + run)
+                        atomicOr(A.err, 1);
                     A.chunks[out++] = ch;
                 }
                 run = 0;
@@ -320,9 +378,12 @@ struct lbm_sim {
     ListParam* lists = nullptr;
     InstParam* insts = nullptr;
     double* amp = nullptr;
+    int64_t NF = 0;                // fluid nodes (outputs); N counts fluid + ghost lattice nodes
+    int64_t nmask = 0;
+    uint32_t* mmask = nullptr;     // missing-population masks of boundary nodes
     int64_t* node_grid = nullptr;  // x-major grid index of each output node (per instance, x-major order)
-    int32_t* out_pos = nullptr;    // output position (x-major rank) of each internal node; null = identity
-    std::vector<int64_t> inst_off; // node offsets, n_inst + 1
+    int32_t* out_pos = nullptr;    // output position (x-major rank) of each lattice node, -1 for ghosts
+    std::vector<int64_t> inst_off; // output (fluid node) offsets, n_inst + 1
     int64_t steps_done = 0;
     // graph replay
     cudaGraphExec_t gexec = nullptr;
@@ -341,15 +402,32 @@ struct lbm_sim {
 namespace {
 
 struct InstBuild {
-    int64_t N = 0;
-    DBuf<int64_t> node_grid;       // x-major grid indices, x-major order
-    DBuf<int32_t> out_pos;         // when the run axis is not z
+    int64_t N = 0;                 // nodes (fluid + ghost)
+    int64_t NF = 0;                // fluid nodes
+    DBuf<int64_t> node_grid;       // x-major grid indices of the fluid points, x-major order
+    DBuf<int32_t> out_pos;         // output position of each node (-1 for ghosts)
     DBuf<Chunk> chunks;
     int64_t nchunks = 0;
+    DBuf<uint32_t> mmask;
+    int64_t nmask = 0;
     std::vector<ZSlot> zslots;
 };
 
-// Chunk count of a geometry for a run axis (set-up heuristic for run_axis 0).
+Vel make_vel(int Q, int ra) {
+    Vel v;
+    v.Q = Q;
+    for (int q = 0; q < Q; ++q) {
+        int c[3];
+        if (Q == 19) { c[0] = Lat<19>::cx(q); c[1] = Lat<19>::cy(q); c[2] = Lat<19>::cz(q); }
+        else { c[0] = Lat<27>::cx(q); c[1] = Lat<27>::cy(q); c[2] = Lat<27>::cz(q); }
+        v.a[q] = (int8_t)c[0];
+        v.b[q] = (int8_t)(ra == 2 ? c[1] : c[2]);
+        v.r[q] = (int8_t)(ra == 2 ? c[2] : c[1]);
+    }
+    return v;
+}
+
+// Number of chunks (fluid runs along the run axis, cut at 32) for a run axis.
 lbm_status count_chunks(const lbm_geometry* g, int ra, cudaStream_t st, int64_t* n) {
     int dims[3];
     geometry_dims(g, dims);
@@ -362,17 +440,31 @@ lbm_status count_chunks(const lbm_geometry* g, int ra, cudaStream_t st, int64_t*
         k_permute_flags<<<blocks_for(npts, 256), 256, 0, st>>>(flags, P, fp.p);
         flags = fp.p;
     }
-    const int64_t ncol = (int64_t)P.Na() * P.Nb();
-    DBuf<int32_t> cc;
+    const Pad D{P.Na(), P.Nb(), P.Nr()};
+    DBuf<uint8_t> type;
+    LBM_TRY(type.alloc(D.cells(), "node types"));
+    k_types<<<blocks_for(D.cells(), 256), 256, 0, st>>>(flags, D, type.p);
+    // chunks only depend on the fluid runs; roles are not needed: count with
+    // a role array of zeros via the fluid cells themselves
+    const int64_t ncol = (int64_t)D.Na * D.Nb;
+    std::vector<int32_t> dummy;
+    DBuf<int32_t> cc, bc, nocell;
+    DBuf<int8_t> zero;
     DBuf<int64_t> co;
     LBM_TRY(cc.alloc(ncol, "chunk counts"));
+    LBM_TRY(bc.alloc(ncol, "boundary counts"));
+    LBM_TRY(nocell.alloc(D.cells(), "node map"));
+    LBM_TRY(zero.alloc(1, "role"));
+    LBM_CUDA(cudaMemsetAsync(nocell.p, 0, sizeof(int32_t) * D.cells(), st));
+    LBM_CUDA(cudaMemsetAsync(zero.p, 0, 1, st));
     LBM_TRY(co.alloc(ncol, "chunk offsets"));
-    k_col_count<<<blocks_for(ncol, 128), 128, 0, st>>>(flags, P.Na(), P.Nb(), P.Nr(), cc.p);
+    k_col_count<<<blocks_for(ncol, 128), 128, 0, st>>>(type.p, nocell.p, zero.p, D, cc.p, bc.p);
     return scan::exclusive_scan(cc.p, ncol, co.p, n, st);
 }
 
-lbm_status build_instance(const lbm_geometry* g, const lbm_sim_params* p, int32_t inst, int ra, int64_t node_off,
-                          int64_t zslot_off, cudaStream_t st, InstBuild& out) {
+lbm_status build_instance(const lbm_geometry* g, const lbm_sim_params* p, int Q, int32_t inst, int ra, int64_t node_off,
+                          int64_t out_off, int64_t zslot_off, int64_t mslot_off, int32_t* d_err, cudaStream_t st,
+                          InstBuild& out) {
     int dims[3];
     geometry_dims(g, dims);
     const Perm P{ra, dims[0], dims[1], dims[2]};
@@ -385,38 +477,39 @@ lbm_status build_instance(const lbm_geometry* g, const lbm_sim_params* p, int32_
         k_permute_flags<<<blocks_for(npts, 256), 256, 0, st>>>(flags, P, fperm.p);
         pflags = fperm.p;
     }
-    // 1. node numbering: compaction of Fluid points in the permuted order
-    int64_t* ng = nullptr;
-    LBM_TRY(scan::compact(pflags, npts, &ng, &out.N, st));
-    DBuf<int64_t> node_perm; node_perm.p = ng;
-    if (out.N == 0) return fail(LBM_ERR_ARG, "instance %d has no fluid node", inst);
-    if (node_off + out.N >= INT32_MAX) return fail(LBM_ERR_ARG, "more than 2^31 nodes");
-    DBuf<int32_t> nop;
-    LBM_TRY(nop.alloc(npts, "node map"));
-    LBM_CUDA(cudaMemsetAsync(nop.p, 0xff, sizeof(int32_t) * npts, st));
-    k_scatter_ids<<<blocks_for(out.N, 256), 256, 0, st>>>(ng, out.N, nop.p);
-    // output order: x-major (the reference's node order, Subdomain.cpp:638-651)
-    if (ra == 2) {
-        out.node_grid.p = node_perm.release();
-    } else {
-        int64_t nx = 0;
+    // 1. fluid + ghost nodes on the padded grid, numbered in permuted order
+    const Pad D{P.Na(), P.Nb(), P.Nr()};
+    DBuf<uint8_t> type;
+    LBM_TRY(type.alloc(D.cells(), "node types"));
+    k_types<<<blocks_for(D.cells(), 256), 256, 0, st>>>(pflags, D, type.p);
+    int64_t* nc = nullptr;
+    LBM_TRY(scan::compact(type.p, D.cells(), &nc, &out.N, st));
+    DBuf<int64_t> node_cell; node_cell.p = nc;
+    if (node_off + out.N >= INT32_MAX) return fail(LBM_ERR_ARG, "more than 2^31 lattice nodes");
+    DBuf<int32_t> noc;
+    LBM_TRY(noc.alloc(D.cells(), "node map"));
+    LBM_CUDA(cudaMemsetAsync(noc.p, 0xff, sizeof(int32_t) * D.cells(), st));
+    k_scatter_ids<<<blocks_for(out.N, 256), 256, 0, st>>>(nc, out.N, noc.p);
+    // 2. outputs in x-major order (the reference's node order, Subdomain.cpp:638-651)
+    {
         int64_t* xg = nullptr;
-        LBM_TRY(scan::compact(flags, npts, &xg, &nx, st));
+        LBM_TRY(scan::compact(flags, npts, &xg, &out.NF, st));
         out.node_grid.p = xg;
+        if (out.NF == 0) return fail(LBM_ERR_ARG, "instance %d has no fluid node", inst);
         DBuf<int32_t> rank;
         LBM_TRY(rank.alloc(npts, "rank map"));
-        k_scatter_ids<<<blocks_for(nx, 256), 256, 0, st>>>(xg, nx, rank.p);
-        k_to_orig<<<blocks_for(out.N, 256), 256, 0, st>>>(node_perm.p, out.N, P);
+        k_scatter_ids<<<blocks_for(out.NF, 256), 256, 0, st>>>(xg, out.NF, rank.p);
         LBM_TRY(out.out_pos.alloc(out.N, "output positions"));
-        k_xrank<<<blocks_for(out.N, 256), 256, 0, st>>>(node_perm.p, out.N, rank.p, node_off, out.out_pos.p);
+        k_out_pos<<<blocks_for(out.N, 256), 256, 0, st>>>(nc, out.N, type.p, D, P, rank.p, out_off, out.out_pos.p);
     }
-    // 2. roles
+    // 3. roles
     DBuf<int8_t> role;
     LBM_TRY(role.alloc(out.N, "node roles"));
-    LBM_CUDA(cudaMemsetAsync(role.p, 0, out.N, st));
+    k_roles_fluid<<<blocks_for(out.N, 256), 256, 0, st>>>(nc, out.N, type.p, role.p);
     const int64_t nb = geometry_nboundary(g);
-    if (nb) k_roles<<<blocks_for(nb, 256), 256, 0, st>>>(geometry_bidx_dev(g), geometry_bmask_dev(g), nb, P, nop.p, role.p);
-    // 3. Zou-He nodes: role list with a boundary-condition kind
+    if (nb)
+        k_roles<<<blocks_for(nb, 256), 256, 0, st>>>(geometry_bidx_dev(g), geometry_bmask_dev(g), nb, P, D, noc.p, role.p);
+    // 4. Zou-He nodes: role list with a boundary-condition kind
     int kind[64] = {0};
     const lbm_list_bc* lbc[64] = {nullptr};
     for (size_t b = 0; b < p->nbcs; ++b) {
@@ -443,20 +536,14 @@ lbm_status build_instance(const lbm_geometry* g, const lbm_sim_params* p, int32_
         std::vector<int8_t> hr(nzn);
         std::vector<int64_t> hid(nzn);
         if (nzn) {
+            std::vector<int32_t> pos(out.N);
+            std::vector<int64_t> ids(nzn);
             LBM_CUDA(cudaMemcpyAsync(hr.data(), zr.p, nzn, cudaMemcpyDeviceToHost, st));
-            if (ra != 2) {
-                std::vector<int32_t> pos(out.N);
-                std::vector<int64_t> ids(nzn);
-                LBM_CUDA(cudaMemcpyAsync(pos.data(), out.out_pos.p, sizeof(int32_t) * out.N, cudaMemcpyDeviceToHost, st));
-                LBM_CUDA(cudaMemcpyAsync(ids.data(), zn, sizeof(int64_t) * nzn, cudaMemcpyDeviceToHost, st));
-                LBM_CUDA(cudaStreamSynchronize(st));
-                for (int64_t s = 0; s < nzn; ++s) hid[s] = pos[ids[s]];
-            } else {
-                LBM_CUDA(cudaMemcpyAsync(hid.data(), zn, sizeof(int64_t) * nzn, cudaMemcpyDeviceToHost, st));
-            }
+            LBM_CUDA(cudaMemcpyAsync(pos.data(), out.out_pos.p, sizeof(int32_t) * out.N, cudaMemcpyDeviceToHost, st));
+            LBM_CUDA(cudaMemcpyAsync(ids.data(), zn, sizeof(int64_t) * nzn, cudaMemcpyDeviceToHost, st));
+            LBM_CUDA(cudaStreamSynchronize(st));
+            for (int64_t s = 0; s < nzn; ++s) hid[s] = pos[ids[s]];
         }
-        LBM_CUDA(cudaStreamSynchronize(st));
-        // rank of each slot within its list in x-major order
         std::vector<int64_t> order(nzn);
         for (int64_t s = 0; s < nzn; ++s) order[s] = s;
         std::sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return hid[a] < hid[b]; });
@@ -486,23 +573,30 @@ lbm_status build_instance(const lbm_geometry* g, const lbm_sim_params* p, int32_
                             (long long)rank[l]);
         }
     }
-    // 4. chunks
-    const int64_t ncol = (int64_t)P.Na() * P.Nb();
-    DBuf<int32_t> ccount;
-    DBuf<int64_t> coff;
+    // 5. chunks and missing masks
+    const int64_t ncol = (int64_t)D.Na * D.Nb;
+    DBuf<int32_t> ccount, bcount;
+    DBuf<int64_t> coff, moff;
     LBM_TRY(ccount.alloc(ncol, "chunk counts"));
+    LBM_TRY(bcount.alloc(ncol, "boundary counts"));
     LBM_TRY(coff.alloc(ncol, "chunk offsets"));
-    k_col_count<<<blocks_for(ncol, 128), 128, 0, st>>>(pflags, P.Na(), P.Nb(), P.Nr(), ccount.p);
+    LBM_TRY(moff.alloc(ncol, "mask offsets"));
+    k_col_count<<<blocks_for(ncol, 128), 128, 0, st>>>(type.p, noc.p, role.p, D, ccount.p, bcount.p);
     LBM_TRY(scan::exclusive_scan(ccount.p, ncol, coff.p, &out.nchunks, st));
+    LBM_TRY(scan::exclusive_scan(bcount.p, ncol, moff.p, &out.nmask, st));
     LBM_TRY(out.chunks.alloc(out.nchunks, "chunks"));
+    LBM_TRY(out.mmask.alloc(out.nmask, "missing masks"));
     FillArgs fa;
-    fa.flags = pflags; fa.Na = P.Na(); fa.Nb = P.Nb(); fa.Nr = P.Nr();
-    fa.chunk_off = coff.p; fa.node_of_point = nop.p; fa.role = role.p;
-    fa.znodes = zn; fa.nz = nzn; fa.node_off = node_off; fa.zslot_off = zslot_off; fa.inst = inst;
-    fa.chunks = out.chunks.p;
+    fa.type = type.p; fa.node_of_cell = noc.p; fa.role = role.p; fa.D = D; fa.V = make_vel(Q, ra);
+    fa.chunk_off = coff.p; fa.mslot_off = moff.p;
+    fa.znodes = zn; fa.nz = nzn; fa.node_off = node_off; fa.zslot_off = zslot_off; fa.mslot_base = mslot_off;
+    fa.inst = inst; fa.chunks = out.chunks.p; fa.mmask = out.mmask.p; fa.err = d_err;
     k_col_fill<<<blocks_for(ncol, 128), 128, 0, st>>>(fa);
     LBM_CUDA(cudaGetLastError());
+    int32_t herr = 0;
+    LBM_CUDA(cudaMemcpyAsync(&herr, d_err, sizeof herr, cudaMemcpyDeviceToHost, st));
     LBM_CUDA(cudaStreamSynchronize(st));
+    if (herr) return fail(LBM_ERR_STATE, "lattice construction: a neighbour column window is not fully populated");
     return LBM_OK;
 }
 
@@ -513,7 +607,8 @@ lbm_status sim_launch(lbm_sim* S, int mode, bool dry, void* src, void* dst, int6
     a.src = src; a.dst = dst; a.stride = S->stride;
     a.zslots = S->zslots; a.lists = S->lists; a.insts = S->insts; a.amp = S->amp;
     a.step = step; a.step_base = step_base;
-    a.out_f = of; a.out_rho = orho; a.out_u = ou; a.out_pos = S->out_pos; a.n_nodes = S->N;
+    a.out_f = of; a.out_rho = orho; a.out_u = ou; a.out_pos = S->out_pos; a.n_nodes = S->NF;
+    a.mmask = S->mmask;
     if (!dry && S->staging == 0) {
         switch (S->store) {
             case ST_F64: return launch_tma_f64(S->Q, mode, S->ra, a, S->err, S->wpb, st);
@@ -633,35 +728,49 @@ lbm_status sim_create(const lbm_geometry* const* g, const lbm_sim_params* p, siz
         }
         S->ra = cy < cz ? 1 : 2;
     }
+    LBM_CUDA(cudaMalloc(&S->err, sizeof(int32_t)));
+    LBM_CUDA(cudaMemsetAsync(S->err, 0, sizeof(int32_t), st));
     std::vector<std::unique_ptr<InstBuild>> builds;
     std::vector<ZSlot> zall;
-    int64_t node_off = 0, nch = 0;
+    int64_t node_off = 0, out_off = 0, nch = 0, nmask = 0;
+    std::vector<int64_t> lat_off(1, 0), chunk_off(1, 0), mask_off(1, 0);
     S->inst_off.push_back(0);
     for (size_t i = 0; i < n; ++i) {
         builds.emplace_back(new InstBuild());
-        LBM_TRY(build_instance(g[i], &p[i], (int32_t)i, S->ra, node_off, (int64_t)zall.size(), st, *builds.back()));
-        node_off += builds.back()->N;
-        nch += builds.back()->nchunks;
-        zall.insert(zall.end(), builds.back()->zslots.begin(), builds.back()->zslots.end());
-        S->inst_off.push_back(node_off);
+        LBM_TRY(build_instance(g[i], &p[i], S->Q, (int32_t)i, S->ra, node_off, out_off, (int64_t)zall.size(), nmask,
+                               S->err, st, *builds.back()));
+        const InstBuild& B = *builds.back();
+        node_off += B.N;
+        out_off += B.NF;
+        nch += B.nchunks;
+        nmask += B.nmask;
+        zall.insert(zall.end(), B.zslots.begin(), B.zslots.end());
+        S->inst_off.push_back(out_off);
+        lat_off.push_back(node_off);
+        chunk_off.push_back(nch);
+        mask_off.push_back(nmask);
     }
     S->N = node_off;
+    S->NF = out_off;
     S->nchunks = nch;
+    S->nmask = nmask;
     S->nz = (int64_t)zall.size();
     // concatenate per-instance arrays
     LBM_CUDA(cudaMalloc(&S->chunks, sizeof(Chunk) * std::max<int64_t>(nch, 1)));
-    LBM_CUDA(cudaMalloc(&S->node_grid, sizeof(int64_t) * S->N));
-    if (S->ra != 2) LBM_CUDA(cudaMalloc(&S->out_pos, sizeof(int32_t) * S->N));
-    int64_t co = 0;
+    LBM_CUDA(cudaMalloc(&S->mmask, sizeof(uint32_t) * std::max<int64_t>(nmask, 1)));
+    LBM_CUDA(cudaMalloc(&S->node_grid, sizeof(int64_t) * S->NF));
+    LBM_CUDA(cudaMalloc(&S->out_pos, sizeof(int32_t) * S->N));
     for (size_t i = 0; i < n; ++i) {
-        LBM_CUDA(cudaMemcpyAsync(S->chunks + co, builds[i]->chunks.p, sizeof(Chunk) * builds[i]->nchunks,
+        const InstBuild& B = *builds[i];
+        LBM_CUDA(cudaMemcpyAsync(S->chunks + chunk_off[i], B.chunks.p, sizeof(Chunk) * B.nchunks,
                                  cudaMemcpyDeviceToDevice, st));
-        LBM_CUDA(cudaMemcpyAsync(S->node_grid + S->inst_off[i], builds[i]->node_grid.p, sizeof(int64_t) * builds[i]->N,
-                                 cudaMemcpyDeviceToDevice, st));
-        if (S->ra != 2)
-            LBM_CUDA(cudaMemcpyAsync(S->out_pos + S->inst_off[i], builds[i]->out_pos.p, sizeof(int32_t) * builds[i]->N,
+        if (B.nmask)
+            LBM_CUDA(cudaMemcpyAsync(S->mmask + mask_off[i], B.mmask.p, sizeof(uint32_t) * B.nmask,
                                      cudaMemcpyDeviceToDevice, st));
-        co += builds[i]->nchunks;
+        LBM_CUDA(cudaMemcpyAsync(S->node_grid + S->inst_off[i], B.node_grid.p, sizeof(int64_t) * B.NF,
+                                 cudaMemcpyDeviceToDevice, st));
+        LBM_CUDA(cudaMemcpyAsync(S->out_pos + lat_off[i], B.out_pos.p, sizeof(int32_t) * B.N, cudaMemcpyDeviceToDevice,
+                                 st));
     }
     LBM_CUDA(cudaMalloc(&S->zslots, sizeof(ZSlot) * std::max<size_t>(zall.size(), 1)));
     if (!zall.empty())
@@ -731,8 +840,6 @@ lbm_status sim_create(const lbm_geometry* const* g, const lbm_sim_params* p, siz
     LBM_CUDA(cudaMalloc(&S->partbad, sizeof(int32_t) * S->part_blocks));
     LBM_CUDA(cudaMalloc(&S->mon, sizeof(MonOut)));
     LBM_CUDA(cudaMalloc(&S->step_base, sizeof(int64_t)));
-    LBM_CUDA(cudaMalloc(&S->err, sizeof(int32_t)));
-    LBM_CUDA(cudaMemsetAsync(S->err, 0, sizeof(int32_t), st));
     LBM_CUDA(cudaGetLastError());
     LBM_CUDA(cudaStreamSynchronize(st));
     lbm_monitors m;
@@ -830,7 +937,7 @@ lbm_status lbm_sim_step(lbm_sim* S, int64_t nsteps, uint32_t flags, void* stream
 lbm_status lbm_sim_info_get(const lbm_sim* S, lbm_sim_info* info) {
     if (!S || !info) return fail(LBM_ERR_ARG, "lbm_sim_info_get: null argument");
     std::memset(info, 0, sizeof *info);
-    info->n_nodes = S->N;
+    info->n_nodes = S->NF;
     info->n_instances = S->n_inst;
     info->steps_done = S->steps_done;
     info->n_chunks = S->nchunks;
@@ -846,26 +953,26 @@ lbm_status lbm_sim_info_get(const lbm_sim* S, lbm_sim_info* info) {
 
 lbm_status lbm_sim_fields(lbm_sim* S, double* rho, double* u, double* f, size_t n_nodes, void* stream) {
     if (!S) return fail(LBM_ERR_ARG, "lbm_sim_fields: null handle");
-    if (n_nodes < (size_t)S->N) return fail(LBM_ERR_ARG, "lbm_sim_fields: capacity %zu < %lld nodes", n_nodes, (long long)S->N);
+    if (n_nodes < (size_t)S->NF) return fail(LBM_ERR_ARG, "lbm_sim_fields: capacity %zu < %lld nodes", n_nodes, (long long)S->NF);
     clear_error();
     cudaStream_t st = (cudaStream_t)stream;
     DBuf<double> df, dr, du;
-    if (f) LBM_TRY(df.alloc((size_t)S->N * S->Q, "field f"));
-    if (rho) LBM_TRY(dr.alloc(S->N, "field rho"));
-    if (u) LBM_TRY(du.alloc((size_t)S->N * 3, "field u"));
+    if (f) LBM_TRY(df.alloc((size_t)S->NF * S->Q, "field f"));
+    if (rho) LBM_TRY(dr.alloc(S->NF, "field rho"));
+    if (u) LBM_TRY(du.alloc((size_t)S->NF * 3, "field u"));
     LBM_TRY(check_timeout(S, st));
     LBM_TRY(sim_dry(S, df.p, dr.p, du.p, false, st));
-    if (f) LBM_CUDA(cudaMemcpyAsync(f, df.p, sizeof(double) * S->N * S->Q, cudaMemcpyDeviceToHost, st));
-    if (rho) LBM_CUDA(cudaMemcpyAsync(rho, dr.p, sizeof(double) * S->N, cudaMemcpyDeviceToHost, st));
-    if (u) LBM_CUDA(cudaMemcpyAsync(u, du.p, sizeof(double) * S->N * 3, cudaMemcpyDeviceToHost, st));
+    if (f) LBM_CUDA(cudaMemcpyAsync(f, df.p, sizeof(double) * S->NF * S->Q, cudaMemcpyDeviceToHost, st));
+    if (rho) LBM_CUDA(cudaMemcpyAsync(rho, dr.p, sizeof(double) * S->NF, cudaMemcpyDeviceToHost, st));
+    if (u) LBM_CUDA(cudaMemcpyAsync(u, du.p, sizeof(double) * S->NF * 3, cudaMemcpyDeviceToHost, st));
     LBM_CUDA(cudaStreamSynchronize(st));
     return LBM_OK;
 }
 
 lbm_status lbm_sim_nodes(const lbm_sim* S, int64_t* grid_index, size_t cap) {
     if (!S || !grid_index) return fail(LBM_ERR_ARG, "lbm_sim_nodes: null argument");
-    if (cap < (size_t)S->N) return fail(LBM_ERR_ARG, "lbm_sim_nodes: capacity %zu < %lld", cap, (long long)S->N);
-    LBM_CUDA(cudaMemcpy(grid_index, S->node_grid, sizeof(int64_t) * S->N, cudaMemcpyDeviceToHost));
+    if (cap < (size_t)S->NF) return fail(LBM_ERR_ARG, "lbm_sim_nodes: capacity %zu < %lld", cap, (long long)S->NF);
+    LBM_CUDA(cudaMemcpy(grid_index, S->node_grid, sizeof(int64_t) * S->NF, cudaMemcpyDeviceToHost));
     return LBM_OK;
 }
 
@@ -899,6 +1006,7 @@ void lbm_sim_destroy(lbm_sim* S) {
     if (S->amp) cudaFree(S->amp);
     if (S->node_grid) cudaFree(S->node_grid);
     if (S->out_pos) cudaFree(S->out_pos);
+    if (S->mmask) cudaFree(S->mmask);
     if (S->part) cudaFree(S->part);
     if (S->partbad) cudaFree(S->partbad);
     if (S->mon) cudaFree(S->mon);

@@ -24,10 +24,9 @@
 // DRY launches run the gather and boundary part only and write f_n, rho_n,
 // u_n in FP64 (snapshots and monitors); they never modify the state.
 //
-// Neighbour addressing: each lane builds, once, a table over the eight
-// neighbouring columns (node id of its same-level neighbour and the fluid
-// bits one below/at/above), so a population's source or destination costs two
-// integer operations; the chunk's own column is a run and needs none.
+// Neighbour addressing: on the ghost-padded run lattice (device.cuh) the
+// source of population q of lane t is K[column] + const + t, one integer add;
+// boundary lanes read a precomputed mask of their missing populations.
 //
 // Arithmetic: Store ST_F64 follows the reference's FP64 expressions operation
 // by operation (its TU is built with -fmad=false), so FP64 runs are bit-exact
@@ -265,21 +264,6 @@ __device__ __forceinline__ void collide(typename Work<S>::T* f, const InstParam&
     }
 }
 
-// Neighbour of a lane at column offset (da, db) and run offset o: existence
-// and node id, from the per-lane table (pb = base + popcount below the lane's
-// own level, bits = fluid at levels -1, 0, +1).
-__device__ __forceinline__ void nbr(const int32_t* pb, const uint32_t* bits, uint32_t own, int32_t n, int da, int db,
-                                    int o, bool& has, int32_t& idx) {
-    if (da == 0 && db == 0) {
-        has = (own >> (1 + o)) & 1u;
-        idx = n + o;
-    } else {
-        const int c = col8(da, db);
-        has = (bits[c] >> (1 + o)) & 1u;
-        idx = pb[c] + (o < 0 ? -(int32_t)(bits[c] & 1u) : (o > 0 ? (int32_t)((bits[c] >> 1) & 1u) : 0));
-    }
-}
-
 struct Partials {
     double* mass;      // per block
     double* inflow;
@@ -288,6 +272,97 @@ struct Partials {
     int32_t* bad;
 };
 
+// Node id of the neighbour of lane `lane` at column offset (da, db) and level
+// offset o (see Chunk): all compile-time except the chunk's bases.
+__device__ __forceinline__ int32_t nb_id(const int32_t* K, int32_t n0, int lane, int da, int db, int o) {
+    return (da == 0 && db == 0 ? n0 - 1 : K[col8(da, db)]) + 1 + o + lane;
+}
+
+// Missing-population mask of a lane (0 for interior lanes).
+__device__ __forceinline__ uint32_t lane_missing(const StepArgs& a, const Chunk* cp, uint32_t bmask, int lane) {
+    if (!((bmask >> lane) & 1u)) return 0u;
+    return __ldg(a.mmask + __ldg(&cp->mslot0) + __popc(bmask & ((1u << lane) - 1u)));
+}
+
+// Fix-ups of missing populations (bounce-back from the node's own post-
+// collision value, or the initial value for populations the reference never
+// rewrites), Zou-He, then collision or snapshot.  Shared by both kernels.
+template <int Q, int S, int MODE, bool DRY>
+__device__ __forceinline__ void node_update(const StepArgs& a, int32_t zslot0, typename Work<S>::T* f, uint32_t missing,
+                                            uint32_t wmask, uint32_t zmask, int lane, int32_t n, int inst, int64_t step,
+                                            double* mon) {
+    using L = Lat<Q>;
+    using T = typename Work<S>::T;
+    const void* A = a.src;
+    if (missing) {
+        const bool wall = (wmask >> lane) & 1u;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            if (!((missing >> q) & 1u)) continue;
+            if (wall && q != L::NO_BB_POP) {
+                if constexpr (MODE == MODE_PULL) f[q] = ld<S, Q, true>(A, a.stride, L::opp(q), n);
+                else if constexpr (MODE == MODE_AA_ODD) f[q] = ld<S, Q>(A, a.stride, q, n);
+                // AA_EVEN: slot q of x already holds f*_{opp q}(x)
+            } else {
+                f[q] = S == ST_F64 ? T(L::w(q)) : T(0);
+            }
+        }
+    }
+    // launch n turns f*(n-1) into f_n: its boundary conditions are those of
+    // reference iteration n-1 (Simulation.cpp:913-915); f_0 is the initial
+    // state, which the reference collides before any boundary condition
+    const bool zl = ((zmask >> lane) & 1u) && step > 0;
+    double zdir = 0.0;
+    if (zl) {
+        const int slot = zslot0 + __popc(zmask & ((1u << lane) - 1u));
+        const ZSlot z = a.zslots[slot];
+        const ListParam lp = a.lists[z.list];
+        T p[Q];
+#pragma unroll
+        for (int q = 0; q < Q; ++q) p[q] = plain<S, Q>(f[q], q);
+        if (z.kind == LBM_BC_VEL_NEGY || z.kind == LBM_BC_VEL_POSX) {
+            const double amp = a.amp[lp.amp_off + (step - 1) % lp.amp_len];
+            const double sc = amp * z.profile;
+            const T v[3] = {T(sc * lp.dir[0]), T(sc * lp.dir[1]), T(sc * lp.dir[2])};
+            if constexpr (Q == 19) {
+                if (z.kind == LBM_BC_VEL_NEGY) zh_vel_negy<T>(p, v);
+            } else {
+                if (z.kind == LBM_BC_VEL_POSX) zh_vel_posx_q27<T>(p, v);
+            }
+            zdir = 1.0;
+        } else {
+            if constexpr (Q == 19) zh_press<T>(p, z.kind, T(lp.rho));
+            zdir = -1.0;
+        }
+#pragma unroll
+        for (int q = 0; q < Q; ++q) f[q] = unplain<S, Q>(p[q], q);
+    }
+    if constexpr (DRY) {
+        double fp[Q];
+#pragma unroll
+        for (int q = 0; q < Q; ++q) fp[q] = (double)plain<S, Q>(f[q], q);
+        double rho, ux, uy, uz;
+        macro_ref<Q, double>(fp, rho, ux, uy, uz);
+        const int64_t pos = (int64_t)a.out_pos[n];
+        if (a.out_f) {
+#pragma unroll
+            for (int q = 0; q < Q; ++q) a.out_f[pos * Q + q] = fp[q];
+        }
+        if (a.out_rho) a.out_rho[pos] = rho;
+        if (a.out_u) { a.out_u[3 * pos] = ux; a.out_u[3 * pos + 1] = uy; a.out_u[3 * pos + 2] = uz; }
+        const double sp = sqrt(ux * ux + uy * uy + uz * uz);
+        mon[0] = rho;
+        mon[3] = sp;
+        mon[4] = (isfinite(rho) && isfinite(sp)) ? 0.0 : 1.0;
+        if (zl) {
+            if (zdir > 0) mon[1] = rho * sp;
+            else mon[2] = rho * sp;
+        }
+    } else {
+        collide<Q, S>(f, a.insts[inst]);
+    }
+}
+
 template <int Q, int S, int MODE, bool DRY, int RA>
 __global__ void __launch_bounds__(256) k_step(StepArgs a, Partials part) {
     using L = Lat<Q>;
@@ -295,8 +370,7 @@ __global__ void __launch_bounds__(256) k_step(StepArgs a, Partials part) {
     using T = typename Work<S>::T;
     const int lane = threadIdx.x & 31;
     const int64_t ci = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-    double m_mass = 0.0, m_in = 0.0, m_out = 0.0, m_maxu = 0.0;
-    int m_bad = 0;
+    double mon[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
     if (ci < a.nchunks) {
         const Chunk* cp = a.chunks + ci;
         const int32_t n0 = __ldg(&cp->n0);
@@ -304,107 +378,32 @@ __global__ void __launch_bounds__(256) k_step(StepArgs a, Partials part) {
         const int len = (int)(li & 63u);
         if (lane < len) {
             const uint32_t wmask = __ldg(&cp->wmask), zmask = __ldg(&cp->zmask), bmask = __ldg(&cp->bmask);
-            const int inst = (int)(li >> 8);
-            const int32_t n = n0 + lane;
-            const bool isb = (bmask >> lane) & 1u;
-            const bool tab = MODE != MODE_AA_EVEN || isb;
-            int32_t pb[8];
-            uint32_t bits[8];
-            if (tab) {
-                const uint64_t lm = (2ull << lane) - 1ull;
+            int32_t K[8];
+            if constexpr (MODE != MODE_AA_EVEN) {
 #pragma unroll
-                for (int c = 0; c < 8; ++c) {
-                    const uint64_t m = __ldg(&cp->mask[c]);
-                    bits[c] = (uint32_t)(m >> lane) & 7u;
-                    pb[c] = __ldg(&cp->base[c]) + __popcll(m & lm);
-                }
+                for (int c = 0; c < 8; ++c) K[c] = __ldg(&cp->K[c]);
             }
-            const uint32_t own = ((lane > 0 || ((li >> 6) & 1u)) ? 1u : 0u) | 2u |
-                                 ((lane < len - 1 || ((li >> 7) & 1u)) ? 4u : 0u);
+            const int32_t n = n0 + lane;
+            const uint32_t missing = lane_missing(a, cp, bmask, lane);
+            const int64_t step = a.step + (a.step_base ? *a.step_base : 0);
             T f[Q];
-            uint32_t missing = 0;
             const void* A = a.src;
 #pragma unroll
             for (int q = 0; q < Q; ++q) {
-                bool has = true;
-                int32_t s = n;
-                if (tab) nbr(pb, bits, own, n, -X::a(q), -X::b(q), -X::r(q), has, s);
-                if (!has) missing |= 1u << q;
+                const bool has = !((missing >> q) & 1u);
                 if constexpr (MODE == MODE_PULL) {
+                    const int32_t s = nb_id(K, n0, lane, -X::a(q), -X::b(q), -X::r(q));
                     f[q] = has ? ld<S, Q, true>(A, a.stride, q, s) : T(0);
                 } else if constexpr (MODE == MODE_AA_EVEN) {
                     f[q] = ld<S, Q>(A, a.stride, q, n);
                 } else {
+                    const int32_t s = nb_id(K, n0, lane, -X::a(q), -X::b(q), -X::r(q));
                     f[q] = has ? ld<S, Q>(A, a.stride, L::opp(q), s) : T(0);
                 }
             }
-            if (missing) {
-                const bool wall = (wmask >> lane) & 1u;
-#pragma unroll
-                for (int q = 0; q < Q; ++q) {
-                    if (!((missing >> q) & 1u)) continue;
-                    if (wall && q != L::NO_BB_POP) {
-                        if constexpr (MODE == MODE_PULL) f[q] = ld<S, Q, true>(A, a.stride, L::opp(q), n);
-                        else if constexpr (MODE == MODE_AA_ODD) f[q] = ld<S, Q>(A, a.stride, q, n);
-                        // AA_EVEN: slot q of x already holds f*_{opp q}(x)
-                    } else {
-                        f[q] = S == ST_F64 ? T(L::w(q)) : T(0);
-                    }
-                }
-            }
-            // launch n turns f*(n-1) into f_n: its boundary conditions are those of
-            // reference iteration n-1 (Simulation.cpp:913-915); f_0 is the initial
-            // state, which the reference collides before any boundary condition
-            const int64_t step = a.step + (a.step_base ? *a.step_base : 0);
-            const bool zl = ((zmask >> lane) & 1u) && step > 0;
-            double zdir = 0.0;
-            if (zl) {
-                const int slot = __ldg(&cp->zslot0) + __popc(zmask & ((1u << lane) - 1u));
-                const ZSlot z = a.zslots[slot];
-                const ListParam lp = a.lists[z.list];
-                T p[Q];
-#pragma unroll
-                for (int q = 0; q < Q; ++q) p[q] = plain<S, Q>(f[q], q);
-                if (z.kind == LBM_BC_VEL_NEGY || z.kind == LBM_BC_VEL_POSX) {
-                    const double amp = a.amp[lp.amp_off + (step - 1) % lp.amp_len];
-                    const double sc = amp * z.profile;
-                    const T v[3] = {T(sc * lp.dir[0]), T(sc * lp.dir[1]), T(sc * lp.dir[2])};
-                    if constexpr (Q == 19) {
-                        if (z.kind == LBM_BC_VEL_NEGY) zh_vel_negy<T>(p, v);
-                    } else {
-                        if (z.kind == LBM_BC_VEL_POSX) zh_vel_posx_q27<T>(p, v);
-                    }
-                    zdir = 1.0;
-                } else {
-                    if constexpr (Q == 19) zh_press<T>(p, z.kind, T(lp.rho));
-                    zdir = -1.0;
-                }
-#pragma unroll
-                for (int q = 0; q < Q; ++q) f[q] = unplain<S, Q>(p[q], q);
-            }
-            if constexpr (DRY) {
-                double fp[Q];
-#pragma unroll
-                for (int q = 0; q < Q; ++q) fp[q] = (double)plain<S, Q>(f[q], q);
-                double rho, ux, uy, uz;
-                macro_ref<Q, double>(fp, rho, ux, uy, uz);
-                const int64_t pos = a.out_pos ? (int64_t)a.out_pos[n] : (int64_t)n;
-                if (a.out_f) {
-#pragma unroll
-                    for (int q = 0; q < Q; ++q) a.out_f[pos * Q + q] = fp[q];
-                }
-                if (a.out_rho) a.out_rho[pos] = rho;
-                if (a.out_u) { a.out_u[3 * pos] = ux; a.out_u[3 * pos + 1] = uy; a.out_u[3 * pos + 2] = uz; }
-                const double sp = sqrt(ux * ux + uy * uy + uz * uz);
-                m_mass = rho;
-                m_maxu = sp;
-                m_bad = (isfinite(rho) && isfinite(sp)) ? 0 : 1;
-                if (zl) {
-                    if (zdir > 0) m_in = rho * sp;
-                    else m_out = rho * sp;
-                }
-            } else {
-                collide<Q, S>(f, a.insts[inst]);
+            node_update<Q, S, MODE, DRY>(a, zmask ? __ldg(&cp->zslot0) : 0, f, missing, wmask, zmask, lane, n,
+                                         (int)(li >> 8), step, mon);
+            if constexpr (!DRY) {
                 void* D = a.dst;
 #pragma unroll
                 for (int q = 0; q < Q; ++q) {
@@ -413,11 +412,8 @@ __global__ void __launch_bounds__(256) k_step(StepArgs a, Partials part) {
                     } else if constexpr (MODE == MODE_AA_EVEN) {
                         st<S, Q>(D, a.stride, L::opp(q), n, f[q]);
                     } else {
-                        bool has;
-                        int32_t d;
-                        nbr(pb, bits, own, n, X::a(q), X::b(q), X::r(q), has, d);
-                        if (has) st<S, Q>(D, a.stride, q, d, f[q]);
-                        else st<S, Q>(D, a.stride, L::opp(q), n, f[q]);
+                        if ((missing >> L::opp(q)) & 1u) st<S, Q>(D, a.stride, L::opp(q), n, f[q]);
+                        else st<S, Q>(D, a.stride, q, nb_id(K, n0, lane, X::a(q), X::b(q), X::r(q)), f[q]);
                     }
                 }
             }
@@ -428,6 +424,8 @@ __global__ void __launch_bounds__(256) k_step(StepArgs a, Partials part) {
             // deterministic block reduction: warp shuffles then thread 0
             __shared__ double sm[4][8];
             __shared__ int sb[8];
+            double m_mass = mon[0], m_in = mon[1], m_out = mon[2], m_maxu = mon[3];
+            int m_bad = mon[4] != 0.0;
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
                 m_mass += __shfl_down_sync(0xffffffffu, m_mass, o);

@@ -34,9 +34,9 @@ template <> struct Slot<ST_BF16S> { static constexpr int EB = 2, EPG = 8, BYTES 
 
 template <int Q, int S>
 struct StageLayout {
-    static constexpr int DESC = 0;          // 128 B chunk descriptor
-    static constexpr int BAR = 128;         // 8 B mbarrier
-    static constexpr int DATA = 144;        // Q slots
+    static constexpr int DESC = 0;          // 64 B chunk descriptor
+    static constexpr int BAR = 64;          // 8 B mbarrier
+    static constexpr int DATA = 80;         // Q slots
     static constexpr int BYTES = (DATA + Q * Slot<S>::BYTES + 15) / 16 * 16;
 };
 
@@ -75,28 +75,16 @@ __device__ __forceinline__ void bulk_g2s(uint32_t dst, const void* src, uint32_t
         : "memory");
 }
 
-// Column (0..7 = col8, 8 = own column) and plane read for population q.
+// Source of population q: column (0..7 = col8, 8 = own), level offset + 1
+// (0..2) and the plane read.  Packed per lane: bits 0-3 column, 4-5 offset,
+// 6-10 plane.
 template <int Q, int RA, int MODE>
-__host__ __device__ constexpr int src_col(int q) {
+__host__ __device__ constexpr uint32_t src_code(int q) {
     using X = Ax<Q, RA>;
-    return (X::a(q) == 0 && X::b(q) == 0) || MODE == MODE_AA_EVEN ? 8 : col8(-X::a(q), -X::b(q));
-}
-template <int Q, int MODE>
-__host__ __device__ constexpr int src_plane(int q) {
-    return MODE == MODE_AA_ODD ? Lat<Q>::opp(q) : q;
-}
-// 4-bit (column) and 5-bit (plane) tables packed in 64-bit words, indexed by lane
-template <int Q, int RA, int MODE>
-__host__ __device__ constexpr uint64_t col_table(int half) {
-    uint64_t t = 0;
-    for (int q = 16 * half; q < Q && q < 16 * half + 16; ++q) t |= (uint64_t)src_col<Q, RA, MODE>(q) << (4 * (q - 16 * half));
-    return t;
-}
-template <int Q, int MODE>
-__host__ __device__ constexpr uint64_t plane_table(int part) {
-    uint64_t t = 0;
-    for (int q = 12 * part; q < Q && q < 12 * part + 12; ++q) t |= (uint64_t)src_plane<Q, MODE>(q) << (5 * (q - 12 * part));
-    return t;
+    if (MODE == MODE_AA_EVEN) return 8u | (1u << 4) | ((uint32_t)q << 6);
+    const int col = (X::a(q) == 0 && X::b(q) == 0) ? 8 : col8(-X::a(q), -X::b(q));
+    const int plane = MODE == MODE_AA_ODD ? Lat<Q>::opp(q) : q;
+    return (uint32_t)col | ((uint32_t)(1 - X::r(q)) << 4) | ((uint32_t)plane << 6);
 }
 
 template <int Q, int S, int MODE, int RA>
@@ -120,49 +108,35 @@ __global__ void __launch_bounds__(256) k_step_tma(StepArgs a, int32_t* err) {
     }
     __syncwarp();
 
-    constexpr uint64_t CT0 = col_table<Q, RA, MODE>(0), CT1 = col_table<Q, RA, MODE>(1);
-    constexpr uint64_t PT0 = plane_table<Q, MODE>(0), PT1 = plane_table<Q, MODE>(1), PT2 = plane_table<Q, MODE>(2);
-    const int my_col = lane < Q ? (int)(((lane < 16 ? CT0 : CT1) >> (4 * (lane & 15))) & 15u) : 8;
-    const int my_plane = lane < Q ? (int)(((lane < 12 ? PT0 : (lane < 24 ? PT1 : PT2)) >> (5 * (lane % 12))) & 31u) : 0;
+    uint32_t code = 0;
+#pragma unroll
+    for (int q = 0; q < Q; ++q)
+        if (lane == q) code = src_code<Q, RA, MODE>(q);
+    const int my_col = (int)(code & 15u), my_o = (int)((code >> 4) & 3u) - 1, my_plane = (int)(code >> 6);
 
-    // Stage chunk c (descriptor word of this lane in dw) into stage s.
+    // Stage chunk (descriptor word `dw` of this lane, lanes 0..15) into stage s.
     auto issue = [&](int s, uint32_t dw) {
         unsigned char* stg = ring + s * LY::BYTES;
-        ((uint32_t*)(stg + LY::DESC))[lane] = dw;
-        const uint32_t n0 = __shfl_sync(0xffffffffu, dw, 0);
-        const uint32_t li = __shfl_sync(0xffffffffu, dw, 1);
-        const int c = lane & 7;
-        const uint32_t b = __shfl_sync(0xffffffffu, dw, 6 + c);
-        const uint32_t mlo = __shfl_sync(0xffffffffu, dw, 14 + 2 * c);
-        const uint32_t mhi = __shfl_sync(0xffffffffu, dw, 15 + 2 * c);
-        int32_t start, cnt;
-        if (lane == 8) {
-            const int e0 = (li >> 6) & 1, e1 = (li >> 7) & 1;
-            start = (int32_t)n0 - e0;
-            cnt = (int32_t)(li & 63u) + e0 + e1;
-        } else {
-            start = (int32_t)b;
-            cnt = __popc(mlo) + __popc(mhi);
-        }
+        if (lane < 16) ((uint32_t*)(stg + LY::DESC))[lane] = dw;
+        const int32_t n0 = (int32_t)__shfl_sync(0xffffffffu, dw, 0);
+        const int len = (int)(__shfl_sync(0xffffffffu, dw, 1) & 63u);
+        const int32_t kc = (int32_t)__shfl_sync(0xffffffffu, dw, 7 + (my_col & 7));
+        const int32_t start = (my_col == 8 ? n0 - 1 : kc) + 1 + my_o;
         const int32_t as = start & ~(SL::EPG - 1);
-        const int32_t ae = (start + cnt + SL::EPG - 1) & ~(SL::EPG - 1);
-        const uint32_t bytes = cnt > 0 ? (uint32_t)(ae - as) * SL::EB : 0u;
-        const int32_t q_as = __shfl_sync(0xffffffffu, as, my_col);
-        const uint32_t q_bytes = __shfl_sync(0xffffffffu, bytes, my_col);
-        const uint32_t mine = lane < Q ? q_bytes : 0u;
+        const int32_t ae = (start + len + SL::EPG - 1) & ~(SL::EPG - 1);
+        const uint32_t mine = lane < Q ? (uint32_t)(ae - as) * SL::EB : 0u;
         const uint32_t total = __reduce_add_sync(0xffffffffu, mine);
         const uint32_t bar = smem_addr(stg + LY::BAR);
         if (lane == 0) mbar_expect_tx(bar, total);
         __syncwarp();
-        if (mine) {
-            bulk_g2s(smem_addr(stg + LY::DATA + lane * SL::BYTES),
-                     gsrc + ((int64_t)my_plane * a.stride + q_as) * SL::EB, mine, bar);
-        }
+        if (mine)
+            bulk_g2s(smem_addr(stg + LY::DATA + lane * SL::BYTES), gsrc + ((int64_t)my_plane * a.stride + as) * SL::EB,
+                     mine, bar);
     };
     auto chunk_of = [&](int64_t k) { return gw + k * G; };
     auto load_desc = [&](int64_t k) -> uint32_t {
         const int64_t c = chunk_of(k);
-        return c < a.nchunks ? __ldg(words + c * 32 + lane) : 0u;
+        return (c < a.nchunks && lane < 16) ? __ldg(words + c * 16 + lane) : 0u;
     };
 
     uint32_t dw = load_desc(0);
@@ -199,58 +173,27 @@ __global__ void __launch_bounds__(256) k_step_tma(StepArgs a, int32_t* err) {
             }
             parity ^= 1u << s;
         }
-        const uint32_t* dsc = (const uint32_t*)(stg + LY::DESC);
-        const Chunk* cp = (const Chunk*)dsc;
+        const Chunk* cp = (const Chunk*)(stg + LY::DESC);
         const int32_t n0 = cp->n0;
         const uint32_t li = cp->len_inst;
         const int len = (int)(li & 63u);
         if (lane < len) {
             const uint32_t wmask = cp->wmask, zmask = cp->zmask, bmask = cp->bmask;
-            const int inst = (int)(li >> 8);
-            const int32_t n = n0 + lane;
-            const bool isb = (bmask >> lane) & 1u;
-            const uint32_t e0 = (li >> 6) & 1u;
-            // per-lane table relative to each staged range
-            int32_t pb[8], rb[8];
-            uint32_t bits[8];
-            const uint64_t lm = (2ull << lane) - 1ull;
+            int32_t K[8];
 #pragma unroll
-            for (int c = 0; c < 8; ++c) {
-                const uint64_t m = cp->mask[c];
-                const int32_t b = cp->base[c];
-                bits[c] = (uint32_t)(m >> lane) & 7u;
-                pb[c] = b + __popcll(m & lm);
-                rb[c] = pb[c] - (b & ~(SL::EPG - 1));
-            }
-            const int32_t own_as = ((int32_t)n0 - (int32_t)e0) & ~(SL::EPG - 1);
-            const uint32_t own = ((lane > 0 || e0) ? 1u : 0u) | 2u | ((lane < len - 1 || ((li >> 7) & 1u)) ? 4u : 0u);
+            for (int c = 0; c < 8; ++c) K[c] = cp->K[c];
+            const int32_t n = n0 + lane;
+            const uint32_t missing =
+                ((bmask >> lane) & 1u) ? __ldg(a.mmask + cp->mslot0 + __popc(bmask & ((1u << lane) - 1u))) : 0u;
             const unsigned char* data = stg + LY::DATA;
             T f[Q];
-            uint32_t missing = 0;
 #pragma unroll
             for (int q = 0; q < Q; ++q) {
-                const int da = MODE == MODE_AA_EVEN ? 0 : -X::a(q), db = MODE == MODE_AA_EVEN ? 0 : -X::b(q);
-                const int o = MODE == MODE_AA_EVEN ? 0 : -X::r(q);
-                bool has;
-                int32_t g, r;
-                if (da == 0 && db == 0) {
-                    has = (own >> (1 + o)) & 1u;
-                    g = n + o;
-                    r = g - own_as;
-                } else {
-                    nbr(pb, bits, own, n, da, db, o, has, g);
-                    r = rb[col8(da, db)] + (g - pb[col8(da, db)]);
-                }
-                if (MODE == MODE_AA_EVEN && isb) {   // a missing source still matters for the fix-ups
-                    bool h2;
-                    int32_t g2;
-                    nbr(pb, bits, own, n, -X::a(q), -X::b(q), -X::r(q), h2, g2);
-                    if (!h2) missing |= 1u << q;
-                } else if (!has) {
-                    missing |= 1u << q;
-                }
+                const bool ev = MODE == MODE_AA_EVEN;
+                const int32_t st0 = ev ? n0 : nb_id(K, n0, 0, -X::a(q), -X::b(q), -X::r(q));
+                const int r = (st0 & (SL::EPG - 1)) + lane;
                 T v = T(0);
-                if (has) {
+                if (ev || !((missing >> q) & 1u)) {
                     const unsigned char* slot = data + q * SL::BYTES;
                     if constexpr (S == ST_F64) v = ((const double*)slot)[r];
                     else if constexpr (S == ST_F32) v = ((const float*)slot)[r] - (float)L::w(q);
@@ -259,43 +202,8 @@ __global__ void __launch_bounds__(256) k_step_tma(StepArgs a, int32_t* err) {
                 }
                 f[q] = v;
             }
-            const void* A = a.src;
-            if (missing) {
-                const bool wall = (wmask >> lane) & 1u;
-#pragma unroll
-                for (int q = 0; q < Q; ++q) {
-                    if (!((missing >> q) & 1u)) continue;
-                    if (wall && q != L::NO_BB_POP) {
-                        if constexpr (MODE == MODE_PULL) f[q] = ld<S, Q, true>(A, a.stride, L::opp(q), n);
-                        else if constexpr (MODE == MODE_AA_ODD) f[q] = ld<S, Q>(A, a.stride, q, n);
-                    } else {
-                        f[q] = S == ST_F64 ? T(L::w(q)) : T(0);
-                    }
-                }
-            }
-            if (((zmask >> lane) & 1u) && step > 0) {
-                const int slot = cp->zslot0 + __popc(zmask & ((1u << lane) - 1u));
-                const ZSlot z = a.zslots[slot];
-                const ListParam lp = a.lists[z.list];
-                T p[Q];
-#pragma unroll
-                for (int q = 0; q < Q; ++q) p[q] = plain<S, Q>(f[q], q);
-                if (z.kind == LBM_BC_VEL_NEGY || z.kind == LBM_BC_VEL_POSX) {
-                    const double amp = a.amp[lp.amp_off + (step - 1) % lp.amp_len];
-                    const double sc = amp * z.profile;
-                    const T v[3] = {T(sc * lp.dir[0]), T(sc * lp.dir[1]), T(sc * lp.dir[2])};
-                    if constexpr (Q == 19) {
-                        if (z.kind == LBM_BC_VEL_NEGY) zh_vel_negy<T>(p, v);
-                    } else {
-                        if (z.kind == LBM_BC_VEL_POSX) zh_vel_posx_q27<T>(p, v);
-                    }
-                } else {
-                    if constexpr (Q == 19) zh_press<T>(p, z.kind, T(lp.rho));
-                }
-#pragma unroll
-                for (int q = 0; q < Q; ++q) f[q] = unplain<S, Q>(p[q], q);
-            }
-            collide<Q, S>(f, a.insts[inst]);
+            double mon[5];
+            node_update<Q, S, MODE, false>(a, cp->zslot0, f, missing, wmask, zmask, lane, n, (int)(li >> 8), step, mon);
             void* D = a.dst;
 #pragma unroll
             for (int q = 0; q < Q; ++q) {
@@ -304,11 +212,8 @@ __global__ void __launch_bounds__(256) k_step_tma(StepArgs a, int32_t* err) {
                 } else if constexpr (MODE == MODE_AA_EVEN) {
                     st<S, Q>(D, a.stride, L::opp(q), n, f[q]);
                 } else {
-                    bool has;
-                    int32_t d;
-                    nbr(pb, bits, own, n, X::a(q), X::b(q), X::r(q), has, d);
-                    if (has) st<S, Q>(D, a.stride, q, d, f[q]);
-                    else st<S, Q>(D, a.stride, L::opp(q), n, f[q]);
+                    if ((missing >> L::opp(q)) & 1u) st<S, Q>(D, a.stride, L::opp(q), n, f[q]);
+                    else st<S, Q>(D, a.stride, q, nb_id(K, n0, lane, X::a(q), X::b(q), X::r(q)), f[q]);
                 }
             }
         }
