@@ -1,0 +1,351 @@
+#!/usr/bin/env python3
+"""Benchmark: D3Q19 MLUPS and HBM-roofline fraction on the 512x1024x512 vascular tree.
+
+Workload (the configuration the headline metric is quoted on): a seeded
+depth-5 binary tree of tubes (root radius 40 lattice units, child/parent
+radius 0.79, branch angles 25-45 deg, ~2.07 M triangles, 32 outlets)
+voxelized on the GPU into a 512 x 1024 x 512 grid (x, y, z; the tree grows
+along -y), D3Q19 BGK, tau 0.6, pulsatile Zou-He inlet
+u(t) = 0.04 (1 + 0.5 sin(2 pi t / 1000)) with a parabolic profile, pressure
+outlets at rho 1.  Synthetic data (seeded generator, no dataset).
+
+GPU arm (default): one step = one fused collide-stream-boundary launch over
+the whole lattice.  `value` is the MLUPS of the FP16-shifted storage path;
+the plain FP32 two-lattice path is timed on the same lattice and reported
+beside it with the ratio, and the velocity error of the FP16 path against the
+FP64 path (bit-exact with the CPU oracle) is stated.  Populations
+(> 300 MB) exceed the 129 MB L2, so no flush is needed between steps.
+
+Reference arm (--impl reference): the PV2013 reference's own step loop
+(Collision, Streaming, ApplyZouHeBc, ApplyWallBc, ApplyOutletBc), compiled
+from its sources, run as one process per host core on a bounded sample of
+the same tree (the inlet section), aggregate MLUPS.
+
+Prints one JSON line (rank 0).  Multi-GPU: independent replicas per rank
+(weak scaling), value = sum over ranks.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "vascular_tree_512x1024x512_D3Q19"
+METRIC = "D3Q19 MLUPS, % HBM roofline: FP16-store & batched vs plain FP32 @ stated err"
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic_bytes_per_node():
+    """DRAM bytes per fluid node per launch of the step kernel, from an ncu
+    capture summarised in profiles/step_kernel_traffic.txt (key = value lines)."""
+    p = os.path.join(ROOT, "profiles", "step_kernel_traffic.txt")
+    out = {}
+    if os.path.exists(p):
+        for line in open(p):
+            if "=" in line and not line.startswith("#"):
+                k, v = line.split("=", 1)
+                try:
+                    out[k.strip()] = float(v.split()[0])
+                except ValueError:
+                    pass
+    return out
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi during a region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.reader = threading.Thread(target=self._read, daemon=True)
+            self.reader.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) >= 8:
+                self.samples.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({n for s in self.samples for n, v in zip(names, s[4:8]) if v.lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def time_steps(sim, steps, warmup, torch):
+    sim.step(warmup, graph=True)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    sim.step(steps, graph=True)
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 1000.0
+
+
+def reference_sample(case):
+    """Inlet section of the tree: 96 x 40 x 96 grid points below the inlet face,
+    node types from the CPU oracle's voxelizer on the full grid's rays."""
+    from oracle import oracle as O
+    bb, dims = O.explicit_grid(case.grid, 1.0)
+    cx, cz = int(case.inlet.center[0]), int(case.inlet.center[1])
+    x0, z0 = cx - 48, cz - 48
+    y1 = int(case.inlet.plane) + 2
+    y0 = y1 - 40
+    block = O.voxelize_columns(case.triangles, bb, 1.0, dims, x0, x0 + 96, y0, y1)
+    sub = block[:, :, z0:z0 + 96].copy()
+    return sub, (float(x0), float(y0), float(z0)), (96, y1 - y0, 96)
+
+
+def run_reference_sample(case, sample, steps, workdir, tag):
+    """One reference process on the sample; returns (fluid nodes, steps, seconds)."""
+    from oracle import oracle as O
+    sub, origin, dims = sample
+    os.makedirs(workdir, exist_ok=True)
+    fpath = os.path.join(workdir, f"flags_{tag}.bin")
+    sub.tofile(fpath)
+    stl = os.path.join(workdir, "one.stl")
+    if not os.path.exists(stl):
+        with open(stl, "w") as fh:
+            fh.write("solid s\nfacet normal 0 0 1\nouter loop\nvertex 0 0 0\nvertex 1 0 0\nvertex 0 1 0\n"
+                     "endloop\nendfacet\nendsolid s\n")
+    plane = case.inlet.plane
+    pred = [(0, (1, repr(float(plane)), 1e-2, (case.inlet.center[0] - 44, math.nan, case.inlet.center[1] - 44),
+                 (case.inlet.center[0] + 44, math.nan, case.inlet.center[1] + 44)))]
+    res = O.run_reference(stl, 1.0, grid=(origin, dims), preds=pred, tau=case.tau, outlet_rho=1.0, steps=steps,
+                          profile=None, amp=None, workdir=os.path.join(workdir, tag), flags_path=fpath)
+    t = res["time"]
+    return t["nodes"], t["steps"], t["seconds"]
+
+
+def reference_arm(args):
+    """The reference's CPU step loop on all host cores (one process per core)."""
+    import numpy as np
+    from concurrent.futures import ThreadPoolExecutor
+    from oracle import oracle as O
+    from pv2013_gb300 import cases
+    if not O.ref_available(19):
+        try:
+            O.build()
+        except Exception:
+            pass
+    if not O.ref_available(19):
+        return {"impl": "reference", "unavailable": "the reference checker (oracle/_ref) could not be built here"}
+    case = cases.vascular_tree(h=2.2)
+    sample = reference_sample(case)
+    cores = os.cpu_count() or 1
+    steps = max(1, min(args.steps, 8))
+    wd = tempfile.mkdtemp(prefix="pv2013_refarm_")
+    for d in range(cores):
+        os.makedirs(os.path.join(wd, f"p{d}"), exist_ok=True)
+    t0 = time.time()
+    with ThreadPoolExecutor(max_workers=cores) as ex:
+        res = list(ex.map(lambda d: run_reference_sample(case, sample, steps, wd, f"p{d}"), range(cores)))
+    wall = time.time() - t0
+    mlups = sum(n * s / sec for n, s, sec in res) / 1e6
+    nodes = res[0][0]
+    return {"metric": METRIC, "value": mlups, "unit": "MLUPS", "impl": "reference", "n_gpus": 0,
+            "steps": steps, "warmup": 0, "higher_is_better": True, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "sample": "inlet section 96x40x96 points", "processes": cores},
+            "cpu_baseline": {"value": mlups, "unit": "MLUPS", "cores": cores, "kind": "reference",
+                             "sample": f"{cores} concurrent reference processes, each {steps} steps on the "
+                                       f"{nodes}-node inlet section of the tree (reference voxelizer bypassed: "
+                                       f"flags from the oracle); step-loop seconds only; wall {wall:.1f}s"},
+            "e2e": {"value": mlups, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def gpu_arm(args, rank, world):
+    import numpy as np
+    import torch
+    from pv2013_gb300 import Reader, Simulation, cases
+    from pv2013_gb300 import engine as E
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    torch.cuda.init()
+    peak, peak_kind = peaks()
+    t0 = time.time()
+    case = cases.vascular_tree(h=2.2)
+    t_mesh = time.time() - t0
+    geom = case.geometry()
+    nf = geom.info.n_fluid
+    specs = case.boundary_specs(geom)
+
+    # --- headline: FP16-shifted storage, AA in-place streaming ---------------
+    sim16 = Simulation(geom, case.tau, specs, precision="f16s", pattern=args.pattern, run_axis=0,
+                       staging=args.staging)
+    info16 = sim16.info()
+    with ClockSampler(dev) as clk:
+        if world > 1:
+            torch.distributed.barrier()
+        sec16 = time_steps(sim16, args.steps, args.warmup, torch)
+    if world > 1:
+        t = torch.tensor([sec16], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        sec16 = float(t.item())
+    mon = sim16.monitors()
+    ms_step = sec16 / args.steps * 1e3
+    mlups16 = nf * args.steps / sec16 / 1e6 * world
+    bpu16 = info16.algorithmic_bytes_per_update
+    del sim16
+
+    # --- plain FP32 two-lattice pull ------------------------------------------
+    sim32 = Simulation(geom, case.tau, specs, precision="f32", pattern="pull", run_axis=0, staging=args.staging)
+    sec32 = time_steps(sim32, args.steps, args.warmup, torch)
+    mlups32 = nf * args.steps / sec32 / 1e6 * world
+    del sim32
+
+    # --- stated error: FP16 vs FP64 (FP64 is bit-exact with the CPU oracle) ----
+    err_steps = args.err_steps
+    s64 = Simulation(geom, case.tau, specs, precision="f64", pattern="pull", run_axis=0)
+    s64.step(err_steps, graph=True)
+    _, r64, u64 = s64.fields(f=False)
+    m64 = s64.monitors()["mass"]
+    del s64
+    s16 = Simulation(geom, case.tau, specs, precision="f16s", pattern=args.pattern, run_axis=0, staging=args.staging)
+    m0 = s16.monitors()["mass"]
+    s16.step(err_steps, graph=True)
+    _, r16, u16 = s16.fields(f=False)
+    m16 = s16.monitors()["mass"]
+    del s16
+    u_l2 = float(np.linalg.norm(u16 - u64) / np.linalg.norm(u64))
+    u_max = float(np.abs(u16 - u64).max() / np.abs(u64).max())
+    rho_drift = float(np.abs(r16 - r64).max())
+    mass_loss_per_1000 = float((m16 - m0) / m0 / err_steps * 1000)
+
+    # --- end to end through the C ABI with host buffers -----------------------
+    e2e_steps = args.steps
+    torch.cuda.synchronize()
+    t0 = time.time()
+    g2 = case.geometry()
+    s2 = Simulation(g2, case.tau, case.boundary_specs(g2), precision="f16s", pattern=args.pattern, run_axis=0,
+                    staging=args.staging)
+    s2.step(e2e_steps, graph=True)
+    _, rho_h, u_h = s2.fields(f=False)
+    torch.cuda.synchronize()
+    e2e_sec = time.time() - t0
+    e2e_mlups = nf * e2e_steps / e2e_sec / 1e6 * world
+    del s2, g2
+    h2d = case.triangles.nbytes + 8 * len(case.inlet_profile(geom)) + 8 * len(case.amp_table())
+    d2h = rho_h.nbytes + u_h.nbytes
+
+    # --- roofline of the step kernel ------------------------------------------
+    launch_s = sec16 / args.steps
+    achieved = bpu16 * nf / launch_s / 1e9
+    tr = profiled_traffic_bytes_per_node()
+    traffic = tr.get("f16s_aa_dram_bytes_per_node")
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": traffic * nf if traffic else None,
+            "peak_kind": peak_kind, "bytes_per_update": bpu16}
+
+    # --- CPU baseline: the reference's step loop on a bounded sample ----------
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        try:
+            from oracle import oracle as O
+            if not O.ref_available(19):
+                O.build()
+            wd = tempfile.mkdtemp(prefix="pv2013_cpu_")
+            n, s, sec = run_reference_sample(case, reference_sample(case), 30, wd, "p0")
+            cpu = {"value": n * s / sec / 1e6, "unit": "MLUPS", "cores": 1, "kind": "reference",
+                   "sample": f"{s} steps of the reference step loop on the {n}-node inlet section (96x40x96) of "
+                             f"the tree, one process"}
+        except Exception as e:  # the CPU baseline is reported, never required
+            cpu = {"value": None, "unit": "MLUPS", "cores": 1, "kind": "reference", "sample": f"failed: {e}"}
+
+    out = {
+        "metric": METRIC, "value": mlups16, "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f16-shifted storage, f32 math", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "grid": [512, 1024, 512], "fluid_nodes": nf, "triangles": len(case.triangles),
+                   "precision": "f16s", "pattern": args.pattern, "run_axis": info16.run_axis,
+                   "staging": "tma" if args.staging == 0 else "direct", "chunks": info16.n_chunks,
+                   "l2": "populations exceed L2 (no flush needed)", "parallelism": f"replicas x{world}"},
+        "fp32_pull_mlups": mlups32, "f16_over_f32": mlups16 / mlups32,
+        "error_vs_fp64": {"steps": err_steps, "u_rel_l2": u_l2, "u_rel_max": u_max, "rho_max_abs": rho_drift,
+                          "mass_change_per_1000_steps": mass_loss_per_1000},
+        "roofline": roof, "cpu_baseline": cpu,
+        "e2e": {"value": e2e_mlups, "unit": "MLUPS", "h2d_bytes_per_step": h2d / e2e_steps,
+                "d2h_bytes_per_step": d2h / e2e_steps,
+                "includes": "STL triangles H2D, GPU voxelization, lattice build, steps, rho/u D2H"},
+        "gpu_launches": args.steps + args.steps // 64 + 2,
+        "voxelize_ms": geom.info.voxelize_ms, "mesh_s": t_mesh,
+        "clocks": clk.summary(), "monitors_after": {k: mon[k] for k in ("mass", "max_speed", "nonfinite")},
+    }
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2000)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    ap.add_argument("--pattern", default="aa", choices=["aa", "pull"])
+    ap.add_argument("--staging", type=int, default=1, help="0 = TMA-staged pipeline, 1 = direct loads")
+    ap.add_argument("--err-steps", type=int, default=500)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        print(json.dumps(reference_arm(args)))
+        return 0
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl")
+    out = gpu_arm(args, rank, world)
+    if rank == 0:
+        print(json.dumps(out))
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

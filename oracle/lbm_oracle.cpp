@@ -149,8 +149,20 @@ static inline bool crosses(double sx, double sy, double pz, double L, const doub
 // test at the ray's (x, y), then the crossing test runs for every z.  The
 // filter is brute force over all triangles unless `binned` is set, in which
 // case a conservative column bin of the triangle's xy box is used.
+int orc_voxelize_cols(const double* tris, int64_t n, const double bbox[6], double spacing, const int dims[3],
+                      int binned, const int cols[4], uint8_t* flags);
+
 int orc_voxelize(const double* tris, int64_t n, const double bbox[6], double spacing, const int dims[3],
                  int binned, uint8_t* flags) {
+    const int cols[4] = {0, dims[0], 0, dims[1]};
+    return orc_voxelize_cols(tris, n, bbox, spacing, dims, binned, cols, flags);
+}
+
+// Same, restricted to the grid columns i in [cols[0], cols[1]), j in
+// [cols[2], cols[3]) (other columns are left untouched); rays, nudges and ray
+// length are those of the full grid.
+int orc_voxelize_cols(const double* tris, int64_t n, const double bbox[6], double spacing, const int dims[3],
+                      int binned, const int cols[4], uint8_t* flags) {
     const int Nx = dims[0], Ny = dims[1], Nz = dims[2];
     const double L = bbox[5] - bbox[4];
     std::vector<std::vector<int64_t>> bins;
@@ -176,6 +188,7 @@ int orc_voxelize(const double* tris, int64_t n, const double bbox[6], double spa
 #pragma omp parallel for schedule(dynamic, 4)
     for (long col = 0; col < (long)Nx * Ny; ++col) {
         int i = (int)(col / Ny), j = (int)(col % Ny);
+        if (i < cols[0] || i >= cols[1] || j < cols[2] || j >= cols[3]) continue;
         double sx = bbox[0] + i * spacing, sy = bbox[2] + j * spacing;
         nudge_xy(sx, sy, bbox);
         std::vector<int64_t> cand;

@@ -51,6 +51,8 @@ def lib():
         L.orc_free.argtypes = [C.c_void_p]
         L.orc_bbox.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_double]
         L.orc_voxelize.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_double, C.c_void_p, C.c_int, C.c_void_p]
+        L.orc_voxelize_cols.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_double, C.c_void_p, C.c_int,
+                                        C.c_void_p, C.c_void_p]
         L.orc_boundary_points.restype = C.c_int64
         L.orc_boundary_points.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64]
         L.orc_classify.argtypes = [C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_double,
@@ -111,6 +113,18 @@ def voxelize(tris, bbox, spacing, dims, binned=True):
     flags = np.zeros(int(np.prod(dims.astype(np.int64))), dtype=np.uint8)
     lib().orc_voxelize(_p(tris), len(tris), _p(bbox), float(spacing), _p(dims), 1 if binned else 0, _p(flags))
     return flags.reshape(tuple(dims))
+
+
+def voxelize_columns(tris, bbox, spacing, dims, i0, i1, j0, j1):
+    """Voxelizes only the columns i in [i0, i1), j in [j0, j1) of the full grid
+    (same rays as the full pass); returns the (i1-i0, j1-j0, Nz) block."""
+    tris = np.ascontiguousarray(tris, dtype=np.float64)
+    bbox = np.ascontiguousarray(bbox, dtype=np.float64)
+    dims = np.ascontiguousarray(dims, dtype=np.int32)
+    flags = np.zeros(int(np.prod(dims.astype(np.int64))), dtype=np.uint8)
+    cols = np.array([i0, i1, j0, j1], dtype=np.int32)
+    lib().orc_voxelize_cols(_p(tris), len(tris), _p(bbox), float(spacing), _p(dims), 1, _p(cols), _p(flags))
+    return flags.reshape(tuple(dims))[i0:i1, j0:j1, :].copy()
 
 
 def boundary_points(flags):
@@ -278,10 +292,16 @@ def ref_available(Q=19):
 
 
 def run_reference(stl_path, spacing, grid=None, preds=(), preset=None, tau=None, outlet_rho=None, steps=0,
-                  profile=None, amp=None, inlet_dir=(0.0, -1.0, 0.0), Q=19, vtk_dir=None, workdir=None):
-    """Runs the reference harness; returns its outputs as numpy arrays."""
+                  profile=None, amp=None, inlet_dir=(0.0, -1.0, 0.0), Q=19, vtk_dir=None, workdir=None,
+                  flags_path=None):
+    """Runs the reference harness; returns its outputs as numpy arrays.  With
+    flags_path the node-type field of the (explicit) grid is read from that file
+    instead of the reference's voxelizer."""
     wd = workdir or tempfile.mkdtemp(prefix="pv2013_ref_")
+    os.makedirs(wd, exist_ok=True)
     lines = [f"stl {stl_path}", f"spacing {spacing!r}"]
+    if flags_path:
+        lines.append(f"flags {flags_path}")
     if grid is not None:
         (mx, my, mz), (nx, ny, nz) = grid
         lines.append(f"box {mx!r} {my!r} {mz!r} {nx} {ny} {nz}")

@@ -25,6 +25,9 @@
 //   inlet_dir <dx> <dy> <dz>   inlet_profile <file of doubles, one per inlet node>
 //   amp_table <file of doubles> amplitude a(t) = table[t mod len]; the inlet
 //                              velocity of node m at step t is (a*p_m)*dir
+//   flags <file>               node-type field (uint8, x-major, 1 = Fluid) of the box
+//                              grid, used instead of labelPoints (for timing the
+//                              step loop on a sample of a large geometry)
 //   out <prefix>               writes <prefix>.flags, .lists, .nodes, .f, .rho, .u
 #include "ComplexGeometry.h"
 #include "LatticeModel.h"
@@ -79,7 +82,7 @@ int main(int argc, char** argv) {
     if (argc < 2) { std::fprintf(stderr, "usage: %s <run file>\n", argv[0]); return 2; }
     MPI_Init(&argc, &argv);
     std::ifstream run(argv[1]);
-    std::string line, stl, out = "ref", vtkdir, profile_path, amp_path;
+    std::string line, stl, out = "ref", vtkdir, profile_path, amp_path, flags_path;
     double spacing = 1.0, tau = 0.8, box[3] = {0, 0, 0};
     int dims[3] = {0, 0, 0}, steps = 0;
     bool have_box = false, preset = false;
@@ -109,6 +112,7 @@ int main(int argc, char** argv) {
         else if (key == "inlet_profile") ss >> profile_path;
         else if (key == "amp_table") ss >> amp_path;
         else if (key == "out") ss >> out;
+        else if (key == "flags") ss >> flags_path;
     }
 
     auto t0 = std::chrono::steady_clock::now();
@@ -131,7 +135,22 @@ int main(int argc, char** argv) {
         std::fprintf(stderr, "box override gives grid %d %d %d\n", G.GeomSize[0], G.GeomSize[1], G.GeomSize[2]);
         return 3;
     }
-    G.labelPoints();
+    if (flags_path.empty()) {
+        G.labelPoints();
+    } else {
+        std::ifstream ff(flags_path, std::ios::binary);
+        const int Nx = G.GeomSize[0], Ny = G.GeomSize[1], Nz = G.GeomSize[2];
+        std::vector<uint8_t> fl((size_t)Nx * Ny * Nz);
+        if (!ff.read(reinterpret_cast<char*>(fl.data()), (std::streamsize)fl.size())) {
+            std::fprintf(stderr, "flags file %s is shorter than the grid\n", flags_path.c_str());
+            return 5;
+        }
+        for (int i = 0; i < Nx; ++i)
+            for (int j = 0; j < Ny; ++j)
+                for (int k = 0; k < Nz; ++k)
+                    G.pointsBox[i][j][k].Type =
+                        fl[((size_t)i * Ny + j) * Nz + k] ? NodeType::Fluid : NodeType::NotFluid;
+    }
     G.boundaryPoints = G.findBoundaryPoints();
     std::vector<Point>* lists[7] = {&G.InletboundaryPoints, &G.OutletboundaryPoints1, &G.OutletboundaryPoints2,
                                     &G.OutletboundaryPoints3, &G.OutletboundaryPoints4, &G.OutletboundaryPoints5,

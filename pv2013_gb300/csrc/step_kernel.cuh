@@ -91,6 +91,22 @@ __device__ __forceinline__ void st(void* base, int64_t stride, int q, int32_t i,
     }
 }
 
+// store to a plane chosen at run time among two (q or opp(q)); the shift
+// applied to FP32 storage is the same for both (w_q = w_opp(q))
+template <int S, int Q>
+__device__ __forceinline__ void st_sel(void* base, int64_t stride, int plane, int q, int32_t i, typename Work<S>::T v) {
+    const int64_t off = (int64_t)plane * stride + i;
+    if constexpr (S == ST_F64) {
+        ((double*)base)[off] = v;
+    } else if constexpr (S == ST_F32) {
+        ((float*)base)[off] = v + (float)Lat<Q>::w(q);
+    } else if constexpr (S == ST_F16S) {
+        ((__half*)base)[off] = __float2half_rn(v);
+    } else {
+        ((__nv_bfloat16*)base)[off] = __float2bfloat16_rn(v);
+    }
+}
+
 // working value <-> plain population
 template <int S, int Q>
 __device__ __forceinline__ typename Work<S>::T plain(typename Work<S>::T v, int q) {
@@ -294,18 +310,20 @@ __device__ __forceinline__ void node_update(const StepArgs& a, int32_t zslot0, t
     using L = Lat<Q>;
     using T = typename Work<S>::T;
     const void* A = a.src;
-    if (missing) {
+    if (__any_sync(__activemask(), missing != 0u)) {
+        // predicated per population, so lanes of a warp do not diverge
         const bool wall = (wmask >> lane) & 1u;
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
-            if (!((missing >> q) & 1u)) continue;
-            if (wall && q != L::NO_BB_POP) {
-                if constexpr (MODE == MODE_PULL) f[q] = ld<S, Q, true>(A, a.stride, L::opp(q), n);
-                else if constexpr (MODE == MODE_AA_ODD) f[q] = ld<S, Q>(A, a.stride, q, n);
-                // AA_EVEN: slot q of x already holds f*_{opp q}(x)
-            } else {
-                f[q] = S == ST_F64 ? T(L::w(q)) : T(0);
+            const bool miss = (missing >> q) & 1u;
+            const bool bb = miss && wall && q != L::NO_BB_POP;
+            if constexpr (MODE == MODE_PULL) {
+                if (bb) f[q] = ld<S, Q, true>(A, a.stride, L::opp(q), n);
+            } else if constexpr (MODE == MODE_AA_ODD) {
+                if (bb) f[q] = ld<S, Q>(A, a.stride, q, n);
             }
+            // AA_EVEN: slot q of x already holds f*_{opp q}(x)
+            if (miss && !bb) f[q] = S == ST_F64 ? T(L::w(q)) : T(0);
         }
     }
     // launch n turns f*(n-1) into f_n: its boundary conditions are those of
@@ -364,7 +382,7 @@ __device__ __forceinline__ void node_update(const StepArgs& a, int32_t zslot0, t
 }
 
 template <int Q, int S, int MODE, bool DRY, int RA>
-__global__ void __launch_bounds__(256) k_step(StepArgs a, Partials part) {
+__global__ void __launch_bounds__(256, 4) k_step(StepArgs a, Partials part) {
     using L = Lat<Q>;
     using X = Ax<Q, RA>;
     using T = typename Work<S>::T;
@@ -412,8 +430,11 @@ __global__ void __launch_bounds__(256) k_step(StepArgs a, Partials part) {
                     } else if constexpr (MODE == MODE_AA_EVEN) {
                         st<S, Q>(D, a.stride, L::opp(q), n, f[q]);
                     } else {
-                        if ((missing >> L::opp(q)) & 1u) st<S, Q>(D, a.stride, L::opp(q), n, f[q]);
-                        else st<S, Q>(D, a.stride, q, nb_id(K, n0, lane, X::a(q), X::b(q), X::r(q)), f[q]);
+                        // branch-free: an absent destination receives the value in the
+                        // node's own opposite slot
+                        const bool back = (missing >> L::opp(q)) & 1u;
+                        const int32_t d = back ? n : nb_id(K, n0, lane, X::a(q), X::b(q), X::r(q));
+                        st_sel<S, Q>(D, a.stride, back ? L::opp(q) : q, q, d, f[q]);
                     }
                 }
             }

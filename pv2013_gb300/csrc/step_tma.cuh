@@ -212,8 +212,9 @@ __global__ void __launch_bounds__(256) k_step_tma(StepArgs a, int32_t* err) {
                 } else if constexpr (MODE == MODE_AA_EVEN) {
                     st<S, Q>(D, a.stride, L::opp(q), n, f[q]);
                 } else {
-                    if ((missing >> L::opp(q)) & 1u) st<S, Q>(D, a.stride, L::opp(q), n, f[q]);
-                    else st<S, Q>(D, a.stride, q, nb_id(K, n0, lane, X::a(q), X::b(q), X::r(q)), f[q]);
+                    const bool back = (missing >> L::opp(q)) & 1u;
+                    const int32_t d = back ? n : nb_id(K, n0, lane, X::a(q), X::b(q), X::r(q));
+                    st_sel<S, Q>(D, a.stride, back ? L::opp(q) : q, q, d, f[q]);
                 }
             }
         }
