@@ -163,8 +163,9 @@ typedef enum lbm_pattern {
     LBM_AUTO = 2     /* chosen by the autotuner */
 } lbm_pattern;
 
-/* Boundary-condition kinds.  The first five are the reference's own routines;
- * the others extend them to the remaining face orientations by symmetry. */
+/* Boundary-condition kinds: the reference's own routines, each for the one
+ * face orientation the reference wrote it for (five D3Q19 routines, one
+ * D3Q27 routine). */
 typedef enum lbm_bc_kind {
     LBM_BC_NONE = 0,            /* list is treated as wall */
     LBM_BC_VEL_NEGY = 1,        /* Boundary::ApplyBc D3Q19, Boundary.cpp:129-148: unknowns -y */

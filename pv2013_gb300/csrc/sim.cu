@@ -3,12 +3,16 @@
 // Simulation driver (Simulation.cpp:3-13, :903-932) for one GPU.
 //
 // Lattice layout in HBM
-//   populations   SoA planes, plane q holds population q of every node
-//                 (node id = x-major order of the fluid points, z fastest);
-//                 plane stride padded to 64 elements (128 B for 16-bit types);
-//                 two planes sets for the pull pattern, one for AA
-//   chunks        one 128-byte descriptor per <=32-node z-run piece (see
-//                 device.cuh): the only per-step index traffic, ~4-6 B/node
+//   nodes         the fluid points plus a one-cell ghost layer around them,
+//                 on the grid padded by one cell on every side, numbered
+//                 with the run axis (y or z) fastest (device.cuh)
+//   populations   SoA planes, plane q holds population q of every node;
+//                 plane stride = node count padded to 64 elements (128 B for
+//                 16-bit storage); two plane sets for the pull pattern, one
+//                 for AA
+//   chunks        one 64-byte descriptor per <=32-node run piece (device.cuh):
+//                 with the missing masks of boundary lanes, the only per-step
+//                 index traffic (~2.5 B per fluid node on a vascular tree)
 //   Zou-He slots  16 B per inlet/outlet node; list and instance tables
 // Node typing follows CreateNodes (Subdomain.cpp:399-477): a boundary point
 // takes the first predicate list that contains it (lowest list id, the
@@ -818,6 +822,9 @@ lbm_status sim_create(const lbm_geometry* const* g, const lbm_sim_params* p, siz
     LBM_CUDA(cudaMemcpyAsync(S->insts, insts.data(), sizeof(InstParam) * n, cudaMemcpyHostToDevice, st));
     // populations, initial f = w (Node.cpp:30-37): stored w for F64/F32, 0 for shifted
     S->stride = (S->N + 63) / 64 * 64;
+    // the step kernels address populations with 32-bit element offsets
+    if ((uint64_t)S->stride * (uint64_t)S->Q > 0xffffffffull)
+        return fail(LBM_ERR_ARG, "lattice of %lld nodes x %d populations exceeds 2^32 values", (long long)S->N, S->Q);
     const int nb = S->pattern == LBM_PULL ? 2 : 1;
     const size_t bytes = (size_t)S->stride * S->Q * store_bytes(S->store);
     std::vector<double> wv(S->Q);

@@ -62,40 +62,44 @@ template <int Q> struct Ax<Q, 1> {   // run axis y: columns (x, z)
 // (the read-only path is used for the pull pattern only: in the AA patterns
 // the kernel writes the array it reads)
 template <int S, int Q, bool RO = false>
-__device__ __forceinline__ typename Work<S>::T ld(const void* base, int64_t stride, int q, int32_t i) {
+__device__ __forceinline__ typename Work<S>::T ld(const void* base, int64_t stride, int q, uint32_t i) {
+    // 32-bit element offset (the lattice holds < 2^32 values)
+    const uint32_t off = (uint32_t)q * (uint32_t)stride + i;
     if constexpr (S == ST_F64) {
-        const double* p = (const double*)base + q * stride + i;
+        const double* p = (const double*)base + off;
         return RO ? __ldg(p) : *p;
     } else if constexpr (S == ST_F32) {
-        const float* p = (const float*)base + q * stride + i;
+        const float* p = (const float*)base + off;
         return (RO ? __ldg(p) : *p) - (float)Lat<Q>::w(q);
     } else if constexpr (S == ST_F16S) {
-        const __half* p = (const __half*)base + q * stride + i;
+        const __half* p = (const __half*)base + off;
         return __half2float(RO ? __ldg(p) : *p);
     } else {
-        const __nv_bfloat16* p = (const __nv_bfloat16*)base + q * stride + i;
+        const __nv_bfloat16* p = (const __nv_bfloat16*)base + off;
         return __bfloat162float(RO ? __ldg(p) : *p);
     }
 }
 
 template <int S, int Q>
-__device__ __forceinline__ void st(void* base, int64_t stride, int q, int32_t i, typename Work<S>::T v) {
+__device__ __forceinline__ void st(void* base, int64_t stride, int q, uint32_t i, typename Work<S>::T v) {
+    const uint32_t off = (uint32_t)q * (uint32_t)stride + i;
     if constexpr (S == ST_F64) {
-        ((double*)base)[q * stride + i] = v;
+        ((double*)base)[off] = v;
     } else if constexpr (S == ST_F32) {
-        ((float*)base)[q * stride + i] = v + (float)Lat<Q>::w(q);
+        ((float*)base)[off] = v + (float)Lat<Q>::w(q);
     } else if constexpr (S == ST_F16S) {
-        ((__half*)base)[q * stride + i] = __float2half_rn(v);
+        ((__half*)base)[off] = __float2half_rn(v);
     } else {
-        ((__nv_bfloat16*)base)[q * stride + i] = __float2bfloat16_rn(v);
+        ((__nv_bfloat16*)base)[off] = __float2bfloat16_rn(v);
     }
 }
 
-// store to a plane chosen at run time among two (q or opp(q)); the shift
-// applied to FP32 storage is the same for both (w_q = w_opp(q))
+// store to slot q of node i, or (back) to slot opp(q) of node n: a select
+// between two 32-bit element offsets (the lattice holds < 2^32 values)
 template <int S, int Q>
-__device__ __forceinline__ void st_sel(void* base, int64_t stride, int plane, int q, int32_t i, typename Work<S>::T v) {
-    const int64_t off = (int64_t)plane * stride + i;
+__device__ __forceinline__ void st_sel(void* base, uint32_t stride, int q, uint32_t i, bool back, uint32_t n,
+                                       typename Work<S>::T v) {
+    const uint32_t off = back ? (uint32_t)Lat<Q>::opp(q) * stride + n : (uint32_t)q * stride + i;
     if constexpr (S == ST_F64) {
         ((double*)base)[off] = v;
     } else if constexpr (S == ST_F32) {
@@ -254,7 +258,7 @@ __device__ __forceinline__ void collide(typename Work<S>::T* f, const InstParam&
             if (L::cz(q)) jz += L::cz(q) > 0 ? f[q] : -f[q];
         }
         const float Krho = K + drho;            // K * rho
-        const float inv = 1.0f / Krho;
+        const float inv = __fdividef(1.0f, Krho);   // Krho > 0 (rho near 1)
         const float ux = jx * inv, uy = jy * inv, uz = jz * inv;
         const float usq15 = 1.5f * (ux * ux + uy * uy + uz * uz);
         const float om = ip.omega_f;
@@ -278,6 +282,15 @@ __device__ __forceinline__ void collide(typename Work<S>::T* f, const InstParam&
             }
         }
     }
+}
+
+// load that the compiler may not merge with an earlier load of the same
+// address, so a value is re-read instead of held in a register across a
+// long stretch of code
+__device__ __forceinline__ int32_t ld_fresh(const int32_t* p) {
+    int32_t v;
+    asm volatile("ld.global.nc.b32 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
 }
 
 struct Partials {
@@ -432,9 +445,12 @@ __global__ void __launch_bounds__(256, 4) k_step(StepArgs a, Partials part) {
                     } else {
                         // branch-free: an absent destination receives the value in the
                         // node's own opposite slot
+                        if (q == 0) {
+#pragma unroll
+                            for (int c = 0; c < 8; ++c) K[c] = ld_fresh(&cp->K[c]);
+                        }
                         const bool back = (missing >> L::opp(q)) & 1u;
-                        const int32_t d = back ? n : nb_id(K, n0, lane, X::a(q), X::b(q), X::r(q));
-                        st_sel<S, Q>(D, a.stride, back ? L::opp(q) : q, q, d, f[q]);
+                        st_sel<S, Q>(D, (uint32_t)a.stride, q, nb_id(K, n0, lane, X::a(q), X::b(q), X::r(q)), back, n, f[q]);
                     }
                 }
             }

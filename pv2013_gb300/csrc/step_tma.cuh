@@ -205,6 +205,11 @@ __global__ void __launch_bounds__(256) k_step_tma(StepArgs a, int32_t* err) {
             double mon[5];
             node_update<Q, S, MODE, false>(a, cp->zslot0, f, missing, wmask, zmask, lane, n, (int)(li >> 8), step, mon);
             void* D = a.dst;
+            if constexpr (MODE == MODE_AA_ODD) {
+                // re-read the bases rather than hold them across the update
+#pragma unroll
+                for (int c = 0; c < 8; ++c) K[c] = ((const volatile int32_t*)cp->K)[c];
+            }
 #pragma unroll
             for (int q = 0; q < Q; ++q) {
                 if constexpr (MODE == MODE_PULL) {
@@ -213,8 +218,7 @@ __global__ void __launch_bounds__(256) k_step_tma(StepArgs a, int32_t* err) {
                     st<S, Q>(D, a.stride, L::opp(q), n, f[q]);
                 } else {
                     const bool back = (missing >> L::opp(q)) & 1u;
-                    const int32_t d = back ? n : nb_id(K, n0, lane, X::a(q), X::b(q), X::r(q));
-                    st_sel<S, Q>(D, a.stride, back ? L::opp(q) : q, q, d, f[q]);
+                    st_sel<S, Q>(D, (uint32_t)a.stride, q, nb_id(K, n0, lane, X::a(q), X::b(q), X::r(q)), back, n, f[q]);
                 }
             }
         }
