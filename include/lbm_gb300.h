@@ -242,6 +242,15 @@ lbm_status lbm_sim_info_get(const lbm_sim* s, lbm_sim_info* info);
  * reference's collision formulas (Simulation.cpp:32-79).  Node order.  Any
  * pointer may be NULL.  For a batch, nodes of all instances are concatenated. */
 lbm_status lbm_sim_fields(lbm_sim* s, double* rho, double* u, double* f, size_t n_nodes, void* stream);
+/* rho and u as lbm_sim_fields gives them, for callers that must not allocate
+ * device memory: the library writes them into one fixed device array of its
+ * own (at most 524288 nodes; larger lattices: LBM_ERR_ARG) and copies them to
+ * the caller's buffers, with no cudaMalloc or cudaFree.  The array is shared
+ * by every call and keeps the last call's values, so calls whose GPU work
+ * overlaps race.  The first call on a device sets the array up (make it
+ * before any stream capture); the handle's device must be current.
+ * No counterpart in the reference. */
+lbm_status lbm_sim_fields_noalloc(lbm_sim* s, double* rho, double* u, size_t n_nodes, void* stream);
 /* Node positions: x-major grid index of every node (per instance, concatenated). */
 lbm_status lbm_sim_nodes(const lbm_sim* s, int64_t* grid_index, size_t cap);
 /* First node of each instance (n_instances+1 offsets). */

@@ -11,6 +11,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "liblbm_gb300.so")
 
 LBM_OK = 0
+ERR_ARG, ERR_STATE = 7, 8
 STATUS_NAMES = {
     0: "LBM_OK", 1: "LBM_ERR_IO", 2: "LBM_ERR_PARSE", 3: "LBM_ERR_NOMEM", 4: "LBM_ERR_CUDA",
     5: "LBM_ERR_DIVERGED", 6: "LBM_ERR_TIMEOUT", 7: "LBM_ERR_ARG", 8: "LBM_ERR_STATE", 9: "LBM_ERR_NODEV",
@@ -100,6 +101,7 @@ PROTOTYPES = {
     "lbm_sim_step": (C.c_int, [C.c_void_p, C.c_int64, C.c_uint32, C.c_void_p]),
     "lbm_sim_info_get": (C.c_int, [C.c_void_p, _P(SimInfo)]),
     "lbm_sim_fields": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
+    "lbm_sim_fields_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
     "lbm_sim_nodes": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "lbm_sim_instance_offsets": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "lbm_sim_monitors": (C.c_int, [C.c_void_p, _P(Monitors), C.c_void_p]),
@@ -129,6 +131,12 @@ def load():
         fn.argtypes = args
     _lib = lib
     return lib
+
+
+def last_error():
+    """Message of the last failing call on this thread."""
+    msg = load().lbm_last_error()
+    return msg.decode() if msg else ""
 
 
 def check(status):

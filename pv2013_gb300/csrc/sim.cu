@@ -22,6 +22,7 @@
 #include <cmath>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -972,6 +973,76 @@ lbm_status lbm_sim_fields(lbm_sim* S, double* rho, double* u, double* f, size_t 
     if (f) LBM_CUDA(cudaMemcpyAsync(f, df.p, sizeof(double) * S->NF * S->Q, cudaMemcpyDeviceToHost, st));
     if (rho) LBM_CUDA(cudaMemcpyAsync(rho, dr.p, sizeof(double) * S->NF, cudaMemcpyDeviceToHost, st));
     if (u) LBM_CUDA(cudaMemcpyAsync(u, du.p, sizeof(double) * S->NF * 3, cudaMemcpyDeviceToHost, st));
+    LBM_CUDA(cudaStreamSynchronize(st));
+    return LBM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Fields without device allocation (lbm_sim_fields_noalloc).
+//
+// lbm_sim_fields takes its FP64 output buffers from cudaMalloc and returns
+// them with cudaFree, and cudaFree waits until the whole device is idle.
+// Callers that sample rho and u while other work keeps the GPU busy -- a time
+// loop or another simulation running on other streams, a lattice sized to
+// fill the device memory, a process whose memory belongs to another
+// allocator -- cannot afford that wait or that allocation.  This variant runs
+// the same snapshot launch of the step kernel into one fixed device array
+// that is part of the library image, so a call allocates nothing.
+//
+// Limits: at most kStaticFieldNodes nodes (rho and u in FP64: 32 B per node,
+// 16 MiB in all); larger lattices are rejected with LBM_ERR_ARG.  Every call,
+// from any handle, uses the same array, and the array keeps what the last
+// call wrote: calls whose GPU work overlaps (other threads, other streams)
+// race on it.  Each call writes every value it copies out (one rho and one u
+// per fluid node), so nothing has to be cleared between calls.
+// The first call on a device looks up the array's device address with that
+// device current (cudaGetSymbolAddress, which may load the module); make that
+// first call before any stream capture.
+static constexpr int64_t kStaticFieldNodes = int64_t(1) << 19;
+static __device__ __align__(256) double g_field_scratch[4 * kStaticFieldNodes];
+
+namespace {
+constexpr int kMaxFieldDevices = 64;
+std::mutex g_field_mu;
+double* g_field_ptr[kMaxFieldDevices] = {};
+
+// device address of g_field_scratch on device `dev` (current), looked up once
+lbm_status field_scratch(int dev, double** out) {
+    std::lock_guard<std::mutex> lock(g_field_mu);
+    if (dev < 0 || dev >= kMaxFieldDevices) return fail(LBM_ERR_ARG, "device %d out of range", dev);
+    if (!g_field_ptr[dev]) {
+        void* p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_field_scratch);
+        if (e != cudaSuccess || !p)
+            return fail(LBM_ERR_CUDA, "cudaGetSymbolAddress(field scratch): %s", cudaGetErrorString(e));
+        g_field_ptr[dev] = (double*)p;
+    }
+    *out = g_field_ptr[dev];
+    return LBM_OK;
+}
+}  // namespace
+
+lbm_status lbm_sim_fields_noalloc(lbm_sim* S, double* rho, double* u, size_t n_nodes, void* stream) {
+    if (!S || !rho || !u) return fail(LBM_ERR_ARG, "lbm_sim_fields_noalloc: null argument");
+    if (S->NF > kStaticFieldNodes)
+        return fail(LBM_ERR_ARG, "lbm_sim_fields_noalloc: %lld nodes exceed the fixed scratch of %lld nodes",
+                    (long long)S->NF, (long long)kStaticFieldNodes);
+    if (n_nodes < (size_t)S->NF)
+        return fail(LBM_ERR_ARG, "lbm_sim_fields_noalloc: capacity %zu < %lld nodes", n_nodes, (long long)S->NF);
+    clear_error();
+    int dev = -1;
+    LBM_CUDA(cudaGetDevice(&dev));
+    if (dev != S->dev)
+        return fail(LBM_ERR_STATE, "lbm_sim_fields_noalloc: device %d is current, the handle lives on %d", dev, S->dev);
+    double* scratch = nullptr;
+    LBM_TRY(field_scratch(dev, &scratch));
+    cudaStream_t st = (cudaStream_t)stream;
+    double* drho = scratch;
+    double* du = scratch + kStaticFieldNodes;
+    LBM_TRY(check_timeout(S, st));
+    LBM_TRY(sim_dry(S, nullptr, drho, du, false, st));
+    LBM_CUDA(cudaMemcpyAsync(rho, drho, sizeof(double) * S->NF, cudaMemcpyDeviceToHost, st));
+    LBM_CUDA(cudaMemcpyAsync(u, du, sizeof(double) * 3 * S->NF, cudaMemcpyDeviceToHost, st));
     LBM_CUDA(cudaStreamSynchronize(st));
     return LBM_OK;
 }
