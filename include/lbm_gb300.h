@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define LBM_ABI_VERSION 1
+#define LBM_ABI_VERSION 2
 
 typedef enum lbm_status {
     LBM_OK = 0,
@@ -204,6 +204,10 @@ typedef struct lbm_sim_params {
                                   1 = y, 2 = z (the reference's x-major order),
                                   0 = the one giving fewer chunks */
     int32_t staging;           /* 0 = TMA-staged pipeline (default), 1 = direct loads */
+    int32_t nodes_per_lane;    /* 1 = one node per lane (staging applies);
+                                  2 = two adjacent nodes per lane with packed
+                                      FP32 arithmetic (FP32 and 16-bit storage,
+                                      direct loads); 0 = default (1) */
 } lbm_sim_params;
 
 typedef struct lbm_sim lbm_sim;
@@ -230,10 +234,13 @@ typedef struct lbm_sim_info {
     int64_t n_nodes;
     int64_t n_instances;
     int64_t steps_done;
-    int64_t n_chunks;
+    int64_t n_chunks;          /* chunks of the step kernel in use */
     int32_t Q, precision, pattern, warps_per_block, run_axis;
     int64_t state_bytes;       /* device bytes of the population arrays */
     double algorithmic_bytes_per_update;  /* 2*Q*storage bytes */
+    int64_t n_lattice_nodes;   /* fluid + ghost nodes (the population arrays' length) */
+    int32_t nodes_per_lane;
+    int32_t reserved;
 } lbm_sim_info;
 lbm_status lbm_sim_info_get(const lbm_sim* s, lbm_sim_info* info);
 

@@ -91,7 +91,7 @@ struct __align__(64) Chunk {
     int32_t zslot0;    // Zou-He slot of the first zmask lane
     int32_t mslot0;    // missing-mask slot of the first bmask lane
     int32_t K[8];      // neighbour columns: node id at level r0-1, index col8(da, db)
-    int32_t pad;
+    uint32_t vmask;    // paired chunks: node slots that are fluid (the others are ghosts)
 };
 static_assert(sizeof(Chunk) == 64, "chunk descriptor is one 64-byte sector pair");
 

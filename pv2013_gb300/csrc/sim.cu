@@ -117,7 +117,9 @@ struct Pad {
     int Na, Nb, Nr;                       // unpadded permuted dims
     __host__ __device__ int64_t Pa() const { return Na + 2; }
     __host__ __device__ int64_t Pb() const { return Nb + 2; }
-    __host__ __device__ int64_t Pr() const { return Nr + 2; }
+    // padded run-axis length, rounded up to even (node ids keep the parity of
+    // their level, which needs every column to end at an odd level)
+    __host__ __device__ int64_t Pr() const { return (Nr + 3) & ~int64_t(1); }
     __host__ __device__ int64_t cells() const { return Pa() * Pb() * Pr(); }
     __host__ __device__ int64_t cell(int64_t a, int64_t b, int64_t r) const { return (a * Pb() + b) * Pr() + r; }
 };
@@ -141,6 +143,21 @@ __global__ void k_types(const uint8_t* __restrict__ pflags, Pad D, uint8_t* __re
                         if (fluid(a + da, b + db, r + dr)) ty = 1;
         }
         type[c] = ty;
+    }
+}
+
+// Extra ghost nodes so that every node id has the parity of its level: one
+// below every segment of consecutive nodes that starts at an odd level and one
+// above every segment that ends at an even level.  Then every segment starts
+// at an even level and has even length, so ids (assigned in cell order) keep
+// id = level (mod 2).  Changing a cell in place never changes another cell's
+// test.
+__global__ void k_parity_ghosts(Pad D, uint8_t* __restrict__ type) {
+    const int64_t n = D.cells();
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+        if (type[c]) continue;
+        const int64_t r = c % D.Pr();
+        if ((r & 1) == 0 ? (r + 1 < D.Pr() && type[c + 1]) : (type[c - 1] != 0)) type[c] = 1;
     }
 }
 
@@ -266,7 +283,7 @@ __global__ void k_col_fill(FillArgs A) {
                     ch.n0 = (int32_t)(A.node_off + n0);
                     ch.len_inst = (uint32_t)run | ((uint32_t)A.inst << 8);
                     ch.wmask = ch.zmask = ch.bmask = 0;
-                    ch.pad = 0;
+                    ch.vmask = run == 32 ? 0xffffffffu : (1u << run) - 1u;
                     ch.mslot0 = (int32_t)(A.mslot_base + ms);
                     for (int t = 0; t < run; ++t) {
                         const int ro = A.role[n0 + t];
@@ -302,6 +319,86 @@ __global__ void k_col_fill(FillArgs A) {
                 }
                 run = 0;
             }
+        }
+    }
+}
+
+// Paired chunks: each fluid run [rf, re] of a column widened to whole pairs
+// [rf & ~1, re | 1] (the added slots are ghost nodes) and cut every 32 slots.
+__global__ void k_col_count2(const uint8_t* __restrict__ type, Pad D, int32_t* __restrict__ nchunk) {
+    const int64_t ncol = (int64_t)D.Na * D.Nb;
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncol; c += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t a = c / D.Nb + 1, b = c % D.Nb + 1;
+        const int64_t base = D.cell(a, b, 0);
+        int32_t nc = 0;
+        int64_t rf = -1;
+        for (int64_t r = 0; r <= D.Pr(); ++r) {
+            const bool fl = r < D.Pr() && type[base + r] == 2;
+            if (fl && rf < 0) rf = r;
+            if (!fl && rf >= 0) {
+                const int64_t r0 = rf & ~int64_t(1), r1 = (r - 1) | 1;
+                nc += (int32_t)((r1 - r0 + 1 + 31) / 32);
+                rf = -1;
+            }
+        }
+        nchunk[c] = nc;
+    }
+}
+
+__global__ void k_col_fill2(FillArgs A) {
+    const Pad& D = A.D;
+    const int64_t ncol = (int64_t)D.Na * D.Nb;
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncol; c += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t a = c / D.Nb + 1, b = c % D.Nb + 1;
+        const int64_t base = D.cell(a, b, 0);
+        int64_t out = A.chunk_off[c];
+        int64_t ms = A.mslot_off[c];
+        int64_t rf = -1;
+        for (int64_t r = 0; r <= D.Pr(); ++r) {
+            const bool fl = r < D.Pr() && A.type[base + r] == 2;
+            if (fl && rf < 0) rf = r;
+            if (fl || rf < 0) continue;
+            const int64_t re = r - 1;
+            const int64_t r1 = re | 1;
+            for (int64_t r0 = rf & ~int64_t(1); r0 <= r1; r0 += 32) {
+                const int len = (int)std::min<int64_t>(32, r1 - r0 + 1);
+                const int64_t lf = std::max(r0, rf), ll = std::min(r0 + len - 1, re);   // fluid levels of the piece
+                Chunk ch;
+                const int32_t n0 = A.node_of_cell[base + r0];
+                ch.n0 = (int32_t)(A.node_off + n0);
+                ch.len_inst = (uint32_t)len | ((uint32_t)A.inst << 8);
+                ch.vmask = ch.wmask = ch.zmask = ch.bmask = 0;
+                ch.mslot0 = (int32_t)(A.mslot_base + ms);
+                if ((n0 & 1) || (r0 & 1) || A.node_of_cell[base + r0 + len - 1] != n0 + len - 1 ||
+                    A.node_of_cell[base + lf - 1] != n0 + (int32_t)(lf - 1 - r0) ||
+                    A.node_of_cell[base + ll + 1] != n0 + (int32_t)(ll + 1 - r0))
+                    atomicOr(A.err, 1);
+                for (int64_t lv = lf; lv <= ll; ++lv) {
+                    const int j = (int)(lv - r0);
+                    ch.vmask |= 1u << j;
+                    const int ro = A.role[n0 + j];
+                    if (ro == 1) ch.wmask |= 1u << j;
+                    if (ro >= 1) { ch.bmask |= 1u << j; ++ms; }
+                }
+                const int64_t zfirst = lower_bound_i64(A.znodes, A.nz, n0);
+                ch.zslot0 = (int32_t)(A.zslot_off + zfirst);
+                for (int64_t zz = zfirst; zz < A.nz && A.znodes[zz] < n0 + len; ++zz)
+                    ch.zmask |= 1u << (int)(A.znodes[zz] - n0);
+                for (int da = -1; da <= 1; ++da)
+                    for (int db = -1; db <= 1; ++db) {
+                        if (da == 0 && db == 0) continue;
+                        // virtual id of level r0-1 such that K + 1 + (level - r0) is the id of
+                        // every level of the fluid window lf-1 .. ll+1 (checked at both ends)
+                        const int32_t kf = A.node_of_cell[D.cell(a + da, b + db, lf - 1)];
+                        const int32_t kl = A.node_of_cell[D.cell(a + da, b + db, ll + 1)];
+                        const int32_t k = kf - (int32_t)(lf - r0);
+                        // (k + 1 is the id of level r0: even, like every id of an even level)
+                        if (kf < 0 || kl != k + 1 + (int32_t)(ll + 1 - r0) || ((k + 1) & 1)) atomicOr(A.err, 1);
+                        ch.K[col8(da, db)] = (int32_t)(A.node_off + (kf < 0 ? 0 : k));
+                    }
+                A.chunks[out++] = ch;
+            }
+            rf = -1;
         }
     }
 }
@@ -370,15 +467,19 @@ int store_bytes(int s) { return s == ST_F64 ? 8 : (s == ST_F32 ? 4 : 2); }
 
 // ---------------------------------------------------------------------------
 
+constexpr int64_t kLatticeSlack = 8;   // even: node ids keep the parity of their level
+
 struct lbm_sim {
     int dev = 0;
-    int Q = 19, store = ST_F64, pattern = LBM_PULL, wpb = 4, ra = 2, staging = 0;
+    int Q = 19, store = ST_F64, pattern = LBM_PULL, wpb = 4, ra = 2, staging = 0, npl = 1;
     int32_t* err = nullptr;        // device flag: a bounded wait in the step kernel gave up
     int64_t N = 0, nchunks = 0, stride = 0, nz = 0;
     int64_t n_inst = 0;
     void* buf[2] = {nullptr, nullptr};
     int cur = 0;                   // pull: buffer holding the current state
     Chunk* chunks = nullptr;
+    Chunk* chunks2 = nullptr;      // paired chunk table (nodes_per_lane = 2)
+    int64_t nchunks2 = 0;
     ZSlot* zslots = nullptr;
     ListParam* lists = nullptr;
     InstParam* insts = nullptr;
@@ -413,6 +514,8 @@ struct InstBuild {
     DBuf<int32_t> out_pos;         // output position of each node (-1 for ghosts)
     DBuf<Chunk> chunks;
     int64_t nchunks = 0;
+    DBuf<Chunk> chunks2;
+    int64_t nchunks2 = 0;
     DBuf<uint32_t> mmask;
     int64_t nmask = 0;
     std::vector<ZSlot> zslots;
@@ -467,9 +570,9 @@ lbm_status count_chunks(const lbm_geometry* g, int ra, cudaStream_t st, int64_t*
     return scan::exclusive_scan(cc.p, ncol, co.p, n, st);
 }
 
-lbm_status build_instance(const lbm_geometry* g, const lbm_sim_params* p, int Q, int32_t inst, int ra, int64_t node_off,
-                          int64_t out_off, int64_t zslot_off, int64_t mslot_off, int32_t* d_err, cudaStream_t st,
-                          InstBuild& out) {
+lbm_status build_instance(const lbm_geometry* g, const lbm_sim_params* p, int Q, int32_t inst, int ra, int npl,
+                          int64_t node_off, int64_t out_off, int64_t zslot_off, int64_t mslot_off, int32_t* d_err,
+                          cudaStream_t st, InstBuild& out) {
     int dims[3];
     geometry_dims(g, dims);
     const Perm P{ra, dims[0], dims[1], dims[2]};
@@ -487,6 +590,7 @@ lbm_status build_instance(const lbm_geometry* g, const lbm_sim_params* p, int Q,
     DBuf<uint8_t> type;
     LBM_TRY(type.alloc(D.cells(), "node types"));
     k_types<<<blocks_for(D.cells(), 256), 256, 0, st>>>(pflags, D, type.p);
+    k_parity_ghosts<<<blocks_for(D.cells(), 256), 256, 0, st>>>(D, type.p);
     int64_t* nc = nullptr;
     LBM_TRY(scan::compact(type.p, D.cells(), &nc, &out.N, st));
     DBuf<int64_t> node_cell; node_cell.p = nc;
@@ -598,6 +702,21 @@ lbm_status build_instance(const lbm_geometry* g, const lbm_sim_params* p, int Q,
     fa.inst = inst; fa.chunks = out.chunks.p; fa.mmask = out.mmask.p; fa.err = d_err;
     k_col_fill<<<blocks_for(ncol, 128), 128, 0, st>>>(fa);
     LBM_CUDA(cudaGetLastError());
+    if (npl == 2) {
+        // paired chunks share the missing masks (same boundary-node order)
+        DBuf<int64_t> coff2;
+        LBM_TRY(coff2.alloc(ncol, "paired chunk offsets"));
+        k_col_count2<<<blocks_for(ncol, 128), 128, 0, st>>>(type.p, D, ccount.p);
+        LBM_TRY(scan::exclusive_scan(ccount.p, ncol, coff2.p, &out.nchunks2, st));
+        LBM_TRY(out.chunks2.alloc(out.nchunks2, "paired chunks"));
+        FillArgs f2 = fa;
+        f2.chunk_off = coff2.p;
+        f2.chunks = out.chunks2.p;
+        f2.mmask = nullptr;
+        k_col_fill2<<<blocks_for(ncol, 128), 128, 0, st>>>(f2);
+        LBM_CUDA(cudaGetLastError());
+        LBM_CUDA(cudaStreamSynchronize(st));   // coff2 is freed on return
+    }
     int32_t herr = 0;
     LBM_CUDA(cudaMemcpyAsync(&herr, d_err, sizeof herr, cudaMemcpyDeviceToHost, st));
     LBM_CUDA(cudaStreamSynchronize(st));
@@ -614,6 +733,15 @@ lbm_status sim_launch(lbm_sim* S, int mode, bool dry, void* src, void* dst, int6
     a.step = step; a.step_base = step_base;
     a.out_f = of; a.out_rho = orho; a.out_u = ou; a.out_pos = S->out_pos; a.n_nodes = S->NF;
     a.mmask = S->mmask;
+    if (!dry && S->npl == 2) {
+        a.chunks = S->chunks2;
+        a.nchunks = S->nchunks2;
+        switch (S->store) {
+            case ST_F32: return launch_pair_f32(S->Q, mode, S->ra, a, S->wpb, st);
+            case ST_F16S: return launch_pair_f16s(S->Q, mode, S->ra, a, S->wpb, st);
+            default: return launch_pair_bf16s(S->Q, mode, S->ra, a, S->wpb, st);
+        }
+    }
     if (!dry && S->staging == 0) {
         switch (S->store) {
             case ST_F64: return launch_tma_f64(S->Q, mode, S->ra, a, S->err, S->wpb, st);
@@ -713,6 +841,10 @@ lbm_status sim_create(const lbm_geometry* const* g, const lbm_sim_params* p, siz
     if (p0.run_axis != 0 && p0.run_axis != 1 && p0.run_axis != 2) return fail(LBM_ERR_ARG, "run_axis must be 0, 1 or 2");
     if (p0.staging != 0 && p0.staging != 1) return fail(LBM_ERR_ARG, "staging must be 0 or 1");
     S->staging = p0.staging;
+    if (p0.nodes_per_lane < 0 || p0.nodes_per_lane > 2) return fail(LBM_ERR_ARG, "nodes_per_lane must be 0, 1 or 2");
+    S->npl = p0.nodes_per_lane == 0 ? 1 : p0.nodes_per_lane;
+    if (S->npl == 2 && S->store == ST_F64)
+        return fail(LBM_ERR_ARG, "nodes_per_lane = 2 needs FP32 or 16-bit storage (FP64 runs one node per lane)");
     for (size_t i = 0; i < n; ++i) {
         if (p[i].Q != p0.Q || p[i].precision != p0.precision || p[i].pattern != p0.pattern)
             return fail(LBM_ERR_ARG, "batch members must share Q, precision and pattern");
@@ -737,38 +869,49 @@ lbm_status sim_create(const lbm_geometry* const* g, const lbm_sim_params* p, siz
     LBM_CUDA(cudaMemsetAsync(S->err, 0, sizeof(int32_t), st));
     std::vector<std::unique_ptr<InstBuild>> builds;
     std::vector<ZSlot> zall;
-    int64_t node_off = 0, out_off = 0, nch = 0, nmask = 0;
-    std::vector<int64_t> lat_off(1, 0), chunk_off(1, 0), mask_off(1, 0);
+    // node ids start at kLatticeSlack and the arrays end kLatticeSlack ids
+    // after the last node: the paired kernel reads up to three ids beyond a
+    // chunk's window for node slots it discards
+    int64_t node_off = kLatticeSlack, out_off = 0, nch = 0, nch2 = 0, nmask = 0;
+    std::vector<int64_t> lat_off(1, node_off), chunk_off(1, 0), chunk2_off(1, 0), mask_off(1, 0);
     S->inst_off.push_back(0);
     for (size_t i = 0; i < n; ++i) {
         builds.emplace_back(new InstBuild());
-        LBM_TRY(build_instance(g[i], &p[i], S->Q, (int32_t)i, S->ra, node_off, out_off, (int64_t)zall.size(), nmask,
-                               S->err, st, *builds.back()));
+        LBM_TRY(build_instance(g[i], &p[i], S->Q, (int32_t)i, S->ra, S->npl, node_off, out_off, (int64_t)zall.size(),
+                               nmask, S->err, st, *builds.back()));
         const InstBuild& B = *builds.back();
         node_off += B.N;
         out_off += B.NF;
         nch += B.nchunks;
+        nch2 += B.nchunks2;
         nmask += B.nmask;
         zall.insert(zall.end(), B.zslots.begin(), B.zslots.end());
         S->inst_off.push_back(out_off);
         lat_off.push_back(node_off);
         chunk_off.push_back(nch);
+        chunk2_off.push_back(nch2);
         mask_off.push_back(nmask);
     }
-    S->N = node_off;
+    S->N = node_off + kLatticeSlack;
     S->NF = out_off;
     S->nchunks = nch;
+    S->nchunks2 = nch2;
     S->nmask = nmask;
     S->nz = (int64_t)zall.size();
     // concatenate per-instance arrays
     LBM_CUDA(cudaMalloc(&S->chunks, sizeof(Chunk) * std::max<int64_t>(nch, 1)));
+    if (S->npl == 2) LBM_CUDA(cudaMalloc(&S->chunks2, sizeof(Chunk) * std::max<int64_t>(nch2, 1)));
     LBM_CUDA(cudaMalloc(&S->mmask, sizeof(uint32_t) * std::max<int64_t>(nmask, 1)));
     LBM_CUDA(cudaMalloc(&S->node_grid, sizeof(int64_t) * S->NF));
     LBM_CUDA(cudaMalloc(&S->out_pos, sizeof(int32_t) * S->N));
+    LBM_CUDA(cudaMemsetAsync(S->out_pos, 0xff, sizeof(int32_t) * S->N, st));
     for (size_t i = 0; i < n; ++i) {
         const InstBuild& B = *builds[i];
         LBM_CUDA(cudaMemcpyAsync(S->chunks + chunk_off[i], B.chunks.p, sizeof(Chunk) * B.nchunks,
                                  cudaMemcpyDeviceToDevice, st));
+        if (S->npl == 2 && B.nchunks2)
+            LBM_CUDA(cudaMemcpyAsync(S->chunks2 + chunk2_off[i], B.chunks2.p, sizeof(Chunk) * B.nchunks2,
+                                     cudaMemcpyDeviceToDevice, st));
         if (B.nmask)
             LBM_CUDA(cudaMemcpyAsync(S->mmask + mask_off[i], B.mmask.p, sizeof(uint32_t) * B.nmask,
                                      cudaMemcpyDeviceToDevice, st));
@@ -802,6 +945,7 @@ lbm_status sim_create(const lbm_geometry* const* g, const lbm_sim_params* p, siz
             L.rho = B.rho;
             for (int a = 0; a < 3; ++a) L.dir[a] = B.dir[a];
             L.amp_off = (int64_t)amp.size() + 1;   // entry 0 of the table is the constant 1
+            if (B.amp_len > 0x7fffffffull) return fail(LBM_ERR_ARG, "bc %zu: amplitude table longer than 2^31", b);
             if (B.amp && B.amp_len) {
                 L.amp_len = (int64_t)B.amp_len;
                 amp.insert(amp.end(), B.amp, B.amp + B.amp_len);
@@ -887,6 +1031,9 @@ lbm_status lbm_batch_create(const lbm_geometry* const* g, const lbm_sim_params* 
 
 lbm_status lbm_sim_step(lbm_sim* S, int64_t nsteps, uint32_t flags, void* stream) {
     if (!S || nsteps < 0) return fail(LBM_ERR_ARG, "lbm_sim_step: bad argument");
+    // the kernels take the inlet waveform phase from a 32-bit step count
+    if (S->steps_done + nsteps > (int64_t)0xffffffffLL)
+        return fail(LBM_ERR_ARG, "lbm_sim_step: a simulation is limited to 2^32 - 1 steps");
     clear_error();
     cudaStream_t st = (cudaStream_t)stream;
     int64_t left = nsteps;
@@ -948,7 +1095,10 @@ lbm_status lbm_sim_info_get(const lbm_sim* S, lbm_sim_info* info) {
     info->n_nodes = S->NF;
     info->n_instances = S->n_inst;
     info->steps_done = S->steps_done;
-    info->n_chunks = S->nchunks;
+    info->n_chunks = S->npl == 2 ? S->nchunks2 : S->nchunks;
+    info->n_lattice_nodes = S->N;
+    info->nodes_per_lane = S->npl;
+    info->reserved = 0;
     info->Q = S->Q;
     info->precision = S->store;
     info->pattern = S->pattern;
@@ -1078,6 +1228,7 @@ void lbm_sim_destroy(lbm_sim* S) {
     free_graph(S);
     for (void* b : S->buf) if (b) cudaFree(b);
     if (S->chunks) cudaFree(S->chunks);
+    if (S->chunks2) cudaFree(S->chunks2);
     if (S->zslots) cudaFree(S->zslots);
     if (S->lists) cudaFree(S->lists);
     if (S->insts) cudaFree(S->insts);

@@ -26,4 +26,10 @@ lbm_status launch_tma_f32(int Q, int mode, int ra, const StepArgs& a, int32_t* e
 lbm_status launch_tma_f16s(int Q, int mode, int ra, const StepArgs& a, int32_t* err, int wpb, cudaStream_t st);
 lbm_status launch_tma_bf16s(int Q, int mode, int ra, const StepArgs& a, int32_t* err, int wpb, cudaStream_t st);
 
+// Paired kernel (two adjacent nodes per lane; non-dry launches, FP32 and
+// 16-bit storage); a.chunks must be the paired chunk table.
+lbm_status launch_pair_f32(int Q, int mode, int ra, const StepArgs& a, int wpb, cudaStream_t st);
+lbm_status launch_pair_f16s(int Q, int mode, int ra, const StepArgs& a, int wpb, cudaStream_t st);
+lbm_status launch_pair_bf16s(int Q, int mode, int ra, const StepArgs& a, int wpb, cudaStream_t st);
+
 }  // namespace lbm

@@ -352,7 +352,8 @@ __device__ __forceinline__ void node_update(const StepArgs& a, int32_t zslot0, t
 #pragma unroll
         for (int q = 0; q < Q; ++q) p[q] = plain<S, Q>(f[q], q);
         if (z.kind == LBM_BC_VEL_NEGY || z.kind == LBM_BC_VEL_POSX) {
-            const double amp = a.amp[lp.amp_off + (step - 1) % lp.amp_len];
+            // 32-bit phase: the step count stays below 2^32 (lbm_sim_step checks)
+            const double amp = a.amp[lp.amp_off + (uint32_t)(step - 1) % (uint32_t)lp.amp_len];
             const double sc = amp * z.profile;
             const T v[3] = {T(sc * lp.dir[0]), T(sc * lp.dir[1]), T(sc * lp.dir[2])};
             if constexpr (Q == 19) {

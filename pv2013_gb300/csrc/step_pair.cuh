@@ -1,0 +1,428 @@
+// Paired step kernel: two adjacent nodes per lane, half a warp per chunk.
+//
+// Same operations and streaming patterns as k_step (step_kernel.cuh), for the
+// FP32 and 16-bit storages; what changes is how a lane covers its nodes:
+//   * lane t of a half-warp owns the nodes at levels r0+2t and r0+2t+1 of its
+//     chunk (a pair).  The lattice numbers every node so that its id has the
+//     parity of its level (sim.cu), so a pair is one aligned 32-bit (16-bit
+//     storage) or 64-bit (FP32 storage) word in each population plane;
+//   * a neighbour pair one level up or down straddles two aligned words: the
+//     lane loads both and takes the high half of one and the low half of the
+//     other (a byte permute, no shuffle);
+//   * the collision runs on packed FP32 pairs (add/sub/mul/fma.rn.f32x2), one
+//     instruction for both nodes;
+//   * boundary fix-ups and Zou-He run per node, only in warps that have them.
+// Chunk pieces start at even levels and hold up to 32 node slots; a slot at
+// either end may be a ghost node (not in the piece's vmask): its values are
+// computed and discarded, and in the AA odd pattern it stores nothing.
+#pragma once
+#include "step.h"
+#include "step_kernel.cuh"
+
+namespace lbm {
+
+// ---------------------------------------------------------------------------
+// packed FP32 pair: node of the lower level in .lo, upper level in .hi
+struct F2 {
+    unsigned long long v;
+};
+__device__ __forceinline__ F2 f2(float lo, float hi) {
+    F2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r.v) : "f"(lo), "f"(hi));
+    return r;
+}
+__device__ __forceinline__ F2 f2s(float a) { return f2(a, a); }
+__device__ __forceinline__ void f2split(F2 a, float& lo, float& hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a.v));
+}
+__device__ __forceinline__ F2 operator+(F2 a, F2 b) {
+    F2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+    return r;
+}
+__device__ __forceinline__ F2 operator-(F2 a, F2 b) {
+    F2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+    return r;
+}
+__device__ __forceinline__ F2 operator*(F2 a, F2 b) {
+    F2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+    return r;
+}
+__device__ __forceinline__ F2 fma2(F2 a, F2 b, F2 c) {
+    F2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r.v) : "l"(a.v), "l"(b.v), "l"(c.v));
+    return r;
+}
+
+// ---------------------------------------------------------------------------
+// storage word of a pair and its conversion to / from working values
+template <int S> struct PairWord;
+template <> struct PairWord<ST_F32> { using W = uint2; };
+template <> struct PairWord<ST_F16S> { using W = uint32_t; };
+template <> struct PairWord<ST_BF16S> { using W = uint32_t; };
+
+template <int S>
+__device__ __forceinline__ typename PairWord<S>::W ldw(const void* base, uint32_t off) {
+    return ((const typename PairWord<S>::W*)base)[off >> 1];
+}
+// high element of word a, low element of word b (a pair one level out of phase)
+template <int S>
+__device__ __forceinline__ typename PairWord<S>::W straddle(typename PairWord<S>::W a, typename PairWord<S>::W b) {
+    if constexpr (S == ST_F32) return make_uint2(a.y, b.x);
+    else return __byte_perm(a, b, 0x5432);
+}
+template <int S, int Q>
+__device__ __forceinline__ F2 unpack(typename PairWord<S>::W w, int q) {
+    if constexpr (S == ST_F32) {
+        const float wq = (float)Lat<Q>::w(q);
+        return f2(__uint_as_float(w.x), __uint_as_float(w.y)) - f2s(wq);
+    } else if constexpr (S == ST_F16S) {
+        const float2 v = __half22float2(*reinterpret_cast<const __half2*>(&w));
+        return f2(v.x, v.y);
+    } else {
+        return f2(__uint_as_float(w << 16), __uint_as_float(w & 0xffff0000u));
+    }
+}
+template <int S, int Q>
+__device__ __forceinline__ typename PairWord<S>::W pack(F2 v, int q) {
+    if constexpr (S == ST_F32) {
+        float lo, hi;
+        f2split(v + f2s((float)Lat<Q>::w(q)), lo, hi);
+        return make_uint2(__float_as_uint(lo), __float_as_uint(hi));
+    } else if constexpr (S == ST_F16S) {
+        float lo, hi;
+        f2split(v, lo, hi);
+        const __half2 h = __floats2half2_rn(lo, hi);
+        return *reinterpret_cast<const uint32_t*>(&h);
+    } else {
+        float lo, hi;
+        f2split(v, lo, hi);
+        const __nv_bfloat162 h = __floats2bfloat162_rn(lo, hi);
+        return *reinterpret_cast<const uint32_t*>(&h);
+    }
+}
+template <int S>
+__device__ __forceinline__ void stw(void* base, uint32_t off, typename PairWord<S>::W w) {
+    ((typename PairWord<S>::W*)base)[off >> 1] = w;
+}
+// one element (one node) of a pair
+template <int S, int Q>
+__device__ __forceinline__ void st_one(void* base, uint32_t off, float v, int q) {
+    if constexpr (S == ST_F32) ((float*)base)[off] = v + (float)Lat<Q>::w(q);
+    else if constexpr (S == ST_F16S) ((__half*)base)[off] = __float2half_rn(v);
+    else ((__nv_bfloat16*)base)[off] = __float2bfloat16_rn(v);
+}
+
+// ---------------------------------------------------------------------------
+// one node (half) of a storage word
+template <int S>
+__device__ __forceinline__ typename PairWord<S>::W take_half(typename PairWord<S>::W w, bool hi,
+                                                           typename PairWord<S>::W src) {
+    if constexpr (S == ST_F32) {
+        if (hi) w.y = src.y; else w.x = src.x;
+        return w;
+    } else {
+        const uint32_t m = hi ? 0xffff0000u : 0x0000ffffu;
+        return (w & ~m) | (src & m);
+    }
+}
+// the value a population keeps when the reference never writes it: w_q
+// (stored unshifted for FP32, as 0 for the shifted formats)
+template <int S, int Q>
+__device__ __forceinline__ typename PairWord<S>::W init_half(typename PairWord<S>::W w, bool hi, int q) {
+    if constexpr (S == ST_F32) {
+        const uint32_t b = __float_as_uint((float)Lat<Q>::w(q));
+        if (hi) w.y = b; else w.x = b;
+        return w;
+    } else {
+        return w & (hi ? 0x0000ffffu : 0xffff0000u);
+    }
+}
+template <int S, int Q>
+__device__ __forceinline__ float half_plain(typename PairWord<S>::W w, bool hi, int q) {
+    float l, h;
+    f2split(unpack<S, Q>(w, q), l, h);
+    return plain<S, Q>(hi ? h : l, q);
+}
+template <int S, int Q>
+__device__ __forceinline__ typename PairWord<S>::W set_half_plain(typename PairWord<S>::W w, bool hi, float p, int q) {
+    const float v = unplain<S, Q>(p, q);
+    if constexpr (S == ST_F32) {
+        const uint32_t b = __float_as_uint(v + (float)Lat<Q>::w(q));
+        if (hi) w.y = b; else w.x = b;
+        return w;
+    } else {
+        uint32_t b;
+        if constexpr (S == ST_F16S) b = __half_as_ushort(__float2half_rn(v));
+        else b = __bfloat16_as_ushort(__float2bfloat16_rn(v));
+        return hi ? ((w & 0x0000ffffu) | (b << 16)) : ((w & 0xffff0000u) | b);
+    }
+}
+
+// Zou-He on one node (half) of the pair words, in FP32 on plain populations;
+// the results are rounded to the storage format before the collision.
+// raw[q * 32] holds population q's word (a warp's words interleaved in
+// shared memory, so the rest of the pair's words need no registers here)
+template <int Q, int S>
+__device__ __forceinline__ void zou_he_half(const StepArgs& a, int slot, typename PairWord<S>::W* raw, bool hi,
+                                            int64_t step) {
+    using T = float;
+    const ZSlot z = a.zslots[slot];
+    const ListParam lp = a.lists[z.list];
+    T p[Q];
+#pragma unroll
+    for (int q = 0; q < Q; ++q) p[q] = half_plain<S, Q>(raw[q * 32], hi, q);
+    if (z.kind == LBM_BC_VEL_NEGY || z.kind == LBM_BC_VEL_POSX) {
+        // 32-bit phase: the step count stays below 2^32 (lbm_sim_step checks)
+            const double amp = a.amp[lp.amp_off + (uint32_t)(step - 1) % (uint32_t)lp.amp_len];
+        const double sc = amp * z.profile;
+        const T v[3] = {T(sc * lp.dir[0]), T(sc * lp.dir[1]), T(sc * lp.dir[2])};
+        if constexpr (Q == 19) {
+            if (z.kind == LBM_BC_VEL_NEGY) zh_vel_negy<T>(p, v);
+        } else {
+            if (z.kind == LBM_BC_VEL_POSX) zh_vel_posx_q27<T>(p, v);
+        }
+    } else {
+        if constexpr (Q == 19) zh_press<T>(p, z.kind, T(lp.rho));
+    }
+#pragma unroll
+    for (int q = 0; q < Q; ++q) raw[q * 32] = set_half_plain<S, Q>(raw[q * 32], hi, p[q], q);
+}
+
+// identity the compiler cannot see through: the relaxation unpacks the words
+// again instead of keeping the first unpacked values alive
+__device__ __forceinline__ uint32_t opaque(uint32_t x) {
+    asm volatile("mov.b32 %0, %0;" : "+r"(x));
+    return x;
+}
+__device__ __forceinline__ uint2 opaque(uint2 x) {
+    asm volatile("mov.b32 %0, %0;" : "+r"(x.x));
+    asm volatile("mov.b32 %0, %0;" : "+r"(x.y));
+    return x;
+}
+
+// ---------------------------------------------------------------------------
+// BGK collision on packed pairs (the FP32 branch of collide(), each operation
+// on both nodes at once).  The populations stay in storage words and are
+// unpacked twice -- for the moments, then for the relaxation -- so that only
+// one word per population is live; emit(q, value) stores each result.
+template <int Q, int S, class Emit>
+__device__ __forceinline__ void collide2(const typename PairWord<S>::W* raw, float om_f, Emit emit) {
+    using L = Lat<Q>;
+    constexpr float K = Work<S>::K;
+    F2 drho, px, nx, py, ny, pz, nz;
+    bool hpx = false, hnx = false, hpy = false, hny = false, hpz = false, hnz = false;
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const F2 v = unpack<S, Q>(raw[q], q);
+        drho = q == 0 ? v : drho + v;
+        if (L::cx(q) > 0) { px = hpx ? px + v : v; hpx = true; }
+        if (L::cx(q) < 0) { nx = hnx ? nx + v : v; hnx = true; }
+        if (L::cy(q) > 0) { py = hpy ? py + v : v; hpy = true; }
+        if (L::cy(q) < 0) { ny = hny ? ny + v : v; hny = true; }
+        if (L::cz(q) > 0) { pz = hpz ? pz + v : v; hpz = true; }
+        if (L::cz(q) < 0) { nz = hnz ? nz + v : v; hnz = true; }
+    }
+    const F2 Krho = drho + f2s(K);
+    float k0, k1;
+    f2split(Krho, k0, k1);
+    const F2 inv = f2(__fdividef(1.0f, k0), __fdividef(1.0f, k1));
+    const F2 ux = (px - nx) * inv, uy = (py - ny) * inv, uz = (pz - nz) * inv;
+    const F2 usq = fma2(uz, uz, fma2(uy, uy, ux * ux));
+    const F2 base = fma2(Krho, usq * f2s(-1.5f), drho);   // K (rho - 1) - 1.5 K rho u^2
+    const F2 Krho45 = Krho * f2s(4.5f);
+    const F2 om = f2s(om_f);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const int o = L::opp(q);
+        const float w = (float)L::w(q);
+        if (o == q) {
+            const F2 v = unpack<S, Q>(opaque(raw[q]), q);
+            emit(q, fma2(om, base * f2s(w) - v, v));
+        } else if (q < o) {
+            F2 cu;
+            bool have = false;
+            if (L::cx(q)) { cu = L::cx(q) > 0 ? ux : f2s(0.f) - ux; have = true; }
+            if (L::cy(q)) { cu = have ? (L::cy(q) > 0 ? cu + uy : cu - uy) : (L::cy(q) > 0 ? uy : f2s(0.f) - uy); have = true; }
+            if (L::cz(q)) { cu = have ? (L::cz(q) > 0 ? cu + uz : cu - uz) : (L::cz(q) > 0 ? uz : f2s(0.f) - uz); have = true; }
+            const F2 sym = fma2(Krho45, cu * cu, base) * f2s(w);
+            const F2 anti = (Krho * f2s(3.0f * w)) * cu;
+            const F2 vq = unpack<S, Q>(opaque(raw[q]), q), vo = unpack<S, Q>(opaque(raw[o]), o);
+            emit(q, fma2(om, (sym + anti) - vq, vq));
+            emit(o, fma2(om, (sym - anti) - vo, vo));
+        }
+    }
+}
+
+// register budget per thread: D3Q19 with 16-bit storage holds one 32-bit
+// word per population: 64 registers (4 blocks of 256) for the node-local and
+// pull patterns, 80 (3 blocks) for the AA odd pattern, which keeps its eight
+// column bases across the collision for the scatter; FP32 storage (two
+// registers per word) and D3Q27 get 128 (2 blocks)
+template <int Q, int S, int MODE> struct PairMinBlocks {
+    static constexpr int value = (Q == 19 && S != ST_F32) ? (MODE == MODE_AA_ODD ? 3 : 4) : 2;
+};
+
+template <int Q, int S, int MODE, int RA>
+__global__ void __launch_bounds__(256, PairMinBlocks<Q, S, MODE>::value) k_step2(StepArgs a) {
+    using L = Lat<Q>;
+    using X = Ax<Q, RA>;
+    using W = typename PairWord<S>::W;
+    const int lane = threadIdx.x & 31;
+    const int t = lane & 15;                      // pair index within the chunk
+    const int64_t ci = ((int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 2 + (lane >> 4);
+    const bool have_chunk = ci < a.nchunks;
+    const Chunk* cp = a.chunks + (have_chunk ? ci : 0);
+    const int32_t n0 = have_chunk ? __ldg(&cp->n0) : 0;
+    const uint32_t li = have_chunk ? __ldg(&cp->len_inst) : 0u;
+    const bool act = have_chunk && 2 * t < (int)(li & 63u);
+    // node slots 2t (lo) and 2t+1 (hi) of the chunk
+    const uint32_t bm_all = act ? __ldg(&cp->bmask) : 0u;
+    const uint32_t zm_all = act ? __ldg(&cp->zmask) : 0u;
+    uint32_t m_lo = 0u, m_hi = 0u;
+    if ((bm_all >> (2 * t)) & 3u) {
+        const int32_t ms = __ldg(&cp->mslot0) + __popc(bm_all & ((1u << (2 * t)) - 1u));
+        if ((bm_all >> (2 * t)) & 1u) m_lo = __ldg(a.mmask + ms);
+        if ((bm_all >> (2 * t + 1)) & 1u) m_hi = __ldg(a.mmask + ms + ((bm_all >> (2 * t)) & 1u));
+    }
+    const uint32_t e = (uint32_t)(n0 + 2 * t);     // id of the lo node (even)
+    const uint32_t st = (uint32_t)a.stride;
+    const int64_t step = a.step + (a.step_base ? *a.step_base : 0);
+    const void* A = a.src;
+
+    W raw[Q];
+    if (act) {
+        int32_t K[8];
+        if constexpr (MODE != MODE_AA_EVEN) {
+#pragma unroll
+            for (int c = 0; c < 8; ++c) K[c] = __ldg(&cp->K[c]);
+        }
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            if constexpr (MODE == MODE_AA_EVEN) {
+                raw[q] = ldw<S>(A, (uint32_t)q * st + e);
+            } else {
+                const int da = -X::a(q), db = -X::b(q), o = -X::r(q);
+                const int plane = MODE == MODE_AA_ODD ? L::opp(q) : q;
+                const uint32_t s = (uint32_t)((da == 0 && db == 0 ? n0 - 1 : K[col8(da, db)]) + 1 + 2 * t);
+                const uint32_t pb = (uint32_t)plane * st;
+                if (o == 0) raw[q] = ldw<S>(A, pb + s);
+                else if (o > 0) raw[q] = straddle<S>(ldw<S>(A, pb + s), ldw<S>(A, pb + s + 2));
+                else raw[q] = straddle<S>(ldw<S>(A, pb + s - 2), ldw<S>(A, pb + s));
+            }
+        }
+    }
+
+    // missing populations (boundary nodes): bounce-back or the initial value
+    if (__any_sync(0xffffffffu, (m_lo | m_hi) != 0u)) {
+        const uint32_t wm = act ? (__ldg(&cp->wmask) >> (2 * t)) & 3u : 0u;
+        const bool w_lo = wm & 1u, w_hi = (wm >> 1) & 1u;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) {
+            const bool ml = (m_lo >> q) & 1u, mh = (m_hi >> q) & 1u;
+            if (ml || mh) {
+                const bool bl = ml && w_lo && q != L::NO_BB_POP, bh = mh && w_hi && q != L::NO_BB_POP;
+                if constexpr (MODE != MODE_AA_EVEN) {
+                    // bounce-back source: own node, slot opp(q) (pull) or slot q (AA odd)
+                    if (bl || bh) {
+                        const int plane = MODE == MODE_PULL ? L::opp(q) : q;
+                        const W own = ldw<S>(A, (uint32_t)plane * st + e);
+                        if (bl) raw[q] = take_half<S>(raw[q], false, own);
+                        if (bh) raw[q] = take_half<S>(raw[q], true, own);
+                    }
+                }
+                // AA even: slot q of x already holds f*_{opp q}(x)
+                if (ml && !bl) raw[q] = init_half<S, Q>(raw[q], false, q);
+                if (mh && !bh) raw[q] = init_half<S, Q>(raw[q], true, q);
+            }
+        }
+    }
+    // Zou-He: launch n applies the boundary conditions of iteration n-1
+    const uint32_t zm = (zm_all >> (2 * t)) & 3u;
+    if (__any_sync(0xffffffffu, zm != 0u && step > 0)) {
+        // the warp's words go through shared memory around the per-node update
+        extern __shared__ __align__(16) unsigned char zsm[];
+        W* buf = (W*)zsm + (threadIdx.x >> 5) * (Q * 32) + lane;
+#pragma unroll
+        for (int q = 0; q < Q; ++q) buf[q * 32] = raw[q];
+        if (step > 0 && zm) {
+            const int z0 = __ldg(&cp->zslot0) + __popc(zm_all & ((1u << (2 * t)) - 1u));
+            if (zm & 1u) zou_he_half<Q, S>(a, z0, buf, false, step);
+            if (zm & 2u) zou_he_half<Q, S>(a, z0 + (int)(zm & 1u), buf, true, step);
+        }
+#pragma unroll
+        for (int q = 0; q < Q; ++q) raw[q] = buf[q * 32];
+    }
+    if (!act) return;
+    void* D = a.dst;
+    const float om = a.insts[li >> 8].omega_f;
+    if constexpr (MODE == MODE_PULL) {
+        collide2<Q, S>(raw, om, [&](int q, F2 v) { stw<S>(D, (uint32_t)q * st + e, pack<S, Q>(v, q)); });
+    } else if constexpr (MODE == MODE_AA_EVEN) {
+        collide2<Q, S>(raw, om, [&](int q, F2 v) { stw<S>(D, (uint32_t)L::opp(q) * st + e, pack<S, Q>(v, q)); });
+    } else {
+        // AA odd: f*_q to slot q of x + c_q, or (absent destination) to slot
+        // opp(q) of x; ghost slots of the pair store nothing
+        const uint32_t vm = (__ldg(&cp->vmask) >> (2 * t)) & 3u;
+        int32_t K[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) K[c] = ld_fresh(&cp->K[c]);
+        collide2<Q, S>(raw, om, [&](int q, F2 v) {
+            const int da = X::a(q), db = X::b(q), o = X::r(q);
+            const uint32_t s = (uint32_t)((da == 0 && db == 0 ? n0 - 1 : K[col8(da, db)]) + 1 + 2 * t);
+            const bool bl = (m_lo >> L::opp(q)) & 1u, bh = (m_hi >> L::opp(q)) & 1u;
+            const uint32_t pq = (uint32_t)q * st, po = (uint32_t)L::opp(q) * st;
+            if (o == 0 && vm == 3u && !bl && !bh) {
+                stw<S>(D, pq + s, pack<S, Q>(v, q));
+            } else {
+                float l, h;
+                f2split(v, l, h);
+                if (vm & 1u) st_one<S, Q>(D, bl ? po + e : pq + s + o, l, q);
+                if (vm & 2u) st_one<S, Q>(D, bh ? po + e + 1 : pq + s + 1 + o, h, q);
+            }
+        });
+    }
+}
+
+// ---------------------------------------------------------------------------
+// launch: two chunks per warp, wpb warps per block
+template <int Q, int S, int MODE, int RA>
+static lbm_status launch_pair_one(const StepArgs& a, int wpb, cudaStream_t st) {
+    // dynamic shared memory: one word per population and lane of each warp
+    // (the Zou-He path); above 48 KB it needs the opt-in attribute
+    static int opted = 0;
+    const size_t smem = (size_t)wpb * Q * 32 * sizeof(typename PairWord<S>::W);
+    if (smem > 48 * 1024 && opted < (int)smem) {
+        const cudaError_t e = cudaFuncSetAttribute(k_step2<Q, S, MODE, RA>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return fail(LBM_ERR_CUDA, "paired step kernel shared memory: %s", cudaGetErrorString(e));
+        opted = (int)smem;
+    }
+    const int64_t per_block = 2 * (int64_t)wpb;
+    const int64_t blocks = (a.nchunks + per_block - 1) / per_block;
+    k_step2<Q, S, MODE, RA><<<(unsigned)(blocks > 0 ? blocks : 1), 32 * wpb, smem, st>>>(a);
+    return LBM_OK;
+}
+
+template <int Q, int S, int RA>
+static lbm_status launch_pair_mode(int mode, const StepArgs& a, int wpb, cudaStream_t st) {
+    if (mode == MODE_PULL) return launch_pair_one<Q, S, MODE_PULL, RA>(a, wpb, st);
+    if (mode == MODE_AA_EVEN) return launch_pair_one<Q, S, MODE_AA_EVEN, RA>(a, wpb, st);
+    return launch_pair_one<Q, S, MODE_AA_ODD, RA>(a, wpb, st);
+}
+
+template <int S>
+static lbm_status launch_pair_store(int Q, int mode, int ra, const StepArgs& a, int wpb, cudaStream_t st) {
+    lbm_status s;
+    if (Q == 19) s = ra == 1 ? launch_pair_mode<19, S, 1>(mode, a, wpb, st) : launch_pair_mode<19, S, 2>(mode, a, wpb, st);
+    else if (Q == 27) s = ra == 1 ? launch_pair_mode<27, S, 1>(mode, a, wpb, st) : launch_pair_mode<27, S, 2>(mode, a, wpb, st);
+    else return fail(LBM_ERR_ARG, "Q must be 19 or 27");
+    if (s != LBM_OK) return s;
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(LBM_ERR_CUDA, "paired step launch: %s", cudaGetErrorString(e));
+    return LBM_OK;
+}
+
+}  // namespace lbm

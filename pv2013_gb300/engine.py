@@ -261,7 +261,7 @@ PRECISIONS = {"f64": _capi.F64, "f32": _capi.F32, "f16s": _capi.F16S, "bf16s": _
 PATTERNS = {"pull": _capi.PULL, "aa": _capi.AA, "auto": _capi.AUTO}
 
 
-def _params(Q, precision, pattern, tau, bcs, warps_per_block, run_axis=0, staging=0):
+def _params(Q, precision, pattern, tau, bcs, warps_per_block, run_axis=0, staging=0, nodes_per_lane=0):
     cb = [b.to_c() for b in bcs]
     arr = (_capi.ListBC * max(len(cb), 1))(*cb)
     p = _capi.SimParams()
@@ -274,6 +274,7 @@ def _params(Q, precision, pattern, tau, bcs, warps_per_block, run_axis=0, stagin
     p.warps_per_block = int(warps_per_block)
     p.run_axis = int(run_axis)
     p.staging = int(staging)
+    p.nodes_per_lane = int(nodes_per_lane)
     return p, arr
 
 
@@ -285,7 +286,7 @@ class Simulation:
     """
 
     def __init__(self, geometry, tau, bcs=(), Q=19, precision="f64", pattern="pull", warps_per_block=0, run_axis=0,
-                 staging=0, stream=None):
+                 staging=0, stream=None, nodes_per_lane=0):
         lib = load()
         self._stream = C.c_void_p(stream) if stream else None
         h = C.c_void_p()
@@ -296,14 +297,14 @@ class Simulation:
             keep = []
             params = (_capi.SimParams * n)()
             for i in range(n):
-                p, arr = _params(Q, precision, pattern, taus[i], bcl[i], warps_per_block, run_axis, staging)
+                p, arr = _params(Q, precision, pattern, taus[i], bcl[i], warps_per_block, run_axis, staging, nodes_per_lane)
                 keep.append((arr, bcl[i]))
                 params[i] = p
             geoms = (C.c_void_p * n)(*[g.handle for g in geometry])
             check(lib.lbm_batch_create(geoms, params, n, self._stream, C.byref(h)))
             self.geometries = list(geometry)
         else:
-            p, arr = _params(Q, precision, pattern, tau, bcs, warps_per_block, run_axis, staging)
+            p, arr = _params(Q, precision, pattern, tau, bcs, warps_per_block, run_axis, staging, nodes_per_lane)
             check(lib.lbm_sim_create(geometry.handle, C.byref(p), self._stream, C.byref(h)))
             self.geometries = [geometry]
         self._h = h

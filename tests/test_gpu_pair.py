@@ -1,0 +1,129 @@
+"""Paired step kernel (two adjacent nodes per lane, packed FP32 arithmetic).
+
+The paired kernel performs the same operations as the one-node-per-lane
+kernel in FP32 (operation order inside the collision differs), so it is
+checked (1) against the FP64 oracle with the reduced-precision tolerances of
+test_gpu_step.py (velocity relative L2 error) and (2) against the
+one-node-per-lane kernel on the same storage: FP32 state within 1e-6
+relative L2 after the test's steps.  Both kernels share the memory layout of
+each streaming pattern, so they may alternate within one run."""
+import numpy as np
+import pytest
+
+from pv2013_gb300 import BoundarySpec, Geometry, Simulation, _capi, cases
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def oracle_u(O, case, geom, steps):
+    geo = O.geometry(case.triangles, case.spacing, case.grid, case.predicates)
+    ref = O.run_case(19, geo, case.tau, {0: (O.BC_VEL_NEGY, 1.0), 2: (O.BC_PRESS_POSY, case.outlet_rho)}, steps,
+                     profile=case.inlet_profile(geom), amp=case.amp_table())
+    return O.macro(ref.f())
+
+
+@pytest.mark.parametrize("precision,tol", [("f32", 2e-5), ("f16s", 1e-3), ("bf16s", 3e-2)])
+@pytest.mark.parametrize("pattern", ["pull", "aa"])
+@pytest.mark.parametrize("run_axis", [1, 2])
+def test_pair_kernel_against_fp64_oracle(oracle_mod, precision, tol, pattern, run_axis):
+    c = cases.pipe()
+    geom = c.geometry()
+    sim = Simulation(geom, c.tau, c.boundary_specs(geom), precision=precision, pattern=pattern, run_axis=run_axis,
+                     nodes_per_lane=2)
+    info = sim.info()
+    assert info.nodes_per_lane == 2 and info.run_axis == run_axis
+    sim.step(400, graph=True)
+    _, rho, u = sim.fields()
+    rr, ur = oracle_u(oracle_mod, c, geom, 400)
+    assert rel_l2(u, ur) < tol, (precision, pattern, rel_l2(u, ur))
+    assert abs(rho.sum() / rr.sum() - 1) < 10 * tol
+
+
+@pytest.mark.parametrize("pattern", ["pull", "aa"])
+@pytest.mark.parametrize("seed", [4000, 4005])
+def test_pair_kernel_matches_single_kernel_fp32(pattern, seed):
+    """Tortuous vessel with a pulsatile inlet: FP32 populations of the paired
+    and the one-node-per-lane kernels agree to FP32 rounding."""
+    c = cases.vessel(seed)
+    geom = c.geometry()
+    runs = []
+    for npl in (1, 2):
+        sim = Simulation(geom, c.tau, c.boundary_specs(geom), precision="f32", pattern=pattern, nodes_per_lane=npl,
+                         staging=1)
+        sim.step(120, graph=True)
+        runs.append(sim.fields())
+    (f1, r1, u1), (f2, r2, u2) = runs
+    assert np.isfinite(f2).all()
+    assert rel_l2(f2, f1) < 1e-6
+    assert rel_l2(u2, u1) < 1e-4
+
+
+def test_pair_kernel_alternates_with_single_kernel():
+    """AA state written by one kernel is read by the other: the layouts agree."""
+    c = cases.vessel(4001)
+    geom = c.geometry()
+    a = Simulation(geom, c.tau, c.boundary_specs(geom), precision="f32", pattern="aa", nodes_per_lane=2)
+    b = Simulation(geom, c.tau, c.boundary_specs(geom), precision="f32", pattern="aa", nodes_per_lane=1, staging=1)
+    a.step(7)
+    b.step(7)
+    assert rel_l2(a.fields()[0], b.fields()[0]) < 1e-6
+
+
+def test_pair_kernel_all_reference_boundaries():
+    """PV2013 geometry (its seven predicate lists, every reference boundary
+    routine): FP32 paired against FP32 one-node-per-lane."""
+    import golden_pv2013 as G
+    from pv2013_gb300 import pv2013_predicates
+    _, tris, _ = G.load()
+    geom = Geometry(tris, 0.1, predicates=pv2013_predicates())
+    kinds = {0: _capi.BC_VEL_NEGY, 1: _capi.BC_PRESS_NEGY, 2: _capi.BC_PRESS_POSY, 3: _capi.BC_PRESS_POSX,
+             4: _capi.BC_PRESS_POSX, 5: _capi.BC_PRESS_POSX, 6: _capi.BC_PRESS_POSZ}
+    specs = [BoundarySpec(0, kinds[0], dir=(0.0, -1.0, 0.0), amp=np.array([0.1]))]
+    specs += [BoundarySpec(l, kinds[l], rho=1.01) for l in range(1, 7)]
+    steps = 6
+    out = {}
+    for npl in (1, 2):
+        sim = Simulation(geom, 0.66, specs, precision="f32", pattern="pull", nodes_per_lane=npl, staging=1)
+        sim.step(steps)
+        out[npl] = sim.fields()
+    assert rel_l2(out[2][0], out[1][0]) < 1e-6
+    assert rel_l2(out[2][2], out[1][2]) < 1e-4
+
+
+def test_pair_kernel_batch_and_d3q27():
+    c1, c2 = cases.pipe(), cases.vessel(4002)
+    g1, g2 = c1.geometry(), c2.geometry()
+    batch = Simulation([g1, g2], [c1.tau, c2.tau], [c1.boundary_specs(g1), c2.boundary_specs(g2)],
+                       precision="f16s", pattern="aa", nodes_per_lane=2)
+    s1 = Simulation(g1, c1.tau, c1.boundary_specs(g1), precision="f16s", pattern="aa", nodes_per_lane=2)
+    s2 = Simulation(g2, c2.tau, c2.boundary_specs(g2), precision="f16s", pattern="aa", nodes_per_lane=2)
+    for s in (batch, s1, s2):
+        s.step(30, graph=True)
+    off = batch.instance_offsets()
+    fb = batch.fields()[0]
+    # the instances are independent: a batch member equals its own run
+    assert np.array_equal(fb[off[0]:off[1]], s1.fields()[0])
+    assert np.array_equal(fb[off[1]:off[2]], s2.fields()[0])
+
+    c = cases.pipe_x()
+    geom = Geometry(c.triangles, 1.0, grid=c.grid, predicates=c.predicates[:1])
+    specs = [BoundarySpec(0, _capi.BC_VEL_POSX, dir=(1.0, 0.0, 0.0), profile=c.inlet_profile(geom),
+                          amp=c.amp_table())]
+    res = {}
+    for npl in (1, 2):
+        sim = Simulation(geom, c.tau, specs, Q=27, precision="f32", pattern="pull", nodes_per_lane=npl, staging=1)
+        sim.step(40)
+        res[npl] = sim.fields()[0]
+    assert rel_l2(res[2], res[1]) < 1e-6
+
+
+def test_pair_kernel_rejects_fp64():
+    c = cases.pipe()
+    geom = c.geometry()
+    with pytest.raises(_capi.LbmError) as e:
+        Simulation(geom, c.tau, c.boundary_specs(geom), precision="f64", nodes_per_lane=2)
+    assert e.value.status == _capi.ERR_ARG
