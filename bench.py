@@ -214,7 +214,7 @@ def gpu_arm(args, rank, world):
 
     # --- headline: FP16-shifted storage, AA in-place streaming ---------------
     sim16 = Simulation(geom, case.tau, specs, precision="f16s", pattern=args.pattern, run_axis=0,
-                       staging=args.staging)
+                       staging=args.staging, nodes_per_lane=args.nodes_per_lane)
     info16 = sim16.info()
     with ClockSampler(dev) as clk:
         if world > 1:
@@ -230,11 +230,17 @@ def gpu_arm(args, rank, world):
     bpu16 = info16.algorithmic_bytes_per_update
     del sim16
 
-    # --- plain FP32 two-lattice pull ------------------------------------------
-    sim32 = Simulation(geom, case.tau, specs, precision="f32", pattern="pull", run_axis=0, staging=args.staging)
+    # --- plain FP32 two-lattice pull: one node per lane, direct loads --------
+    sim32 = Simulation(geom, case.tau, specs, precision="f32", pattern="pull", run_axis=0, staging=1,
+                       nodes_per_lane=1)
     sec32 = time_steps(sim32, args.steps, args.warmup, torch)
     mlups32 = nf * args.steps / sec32 / 1e6 * world
     del sim32
+    # the same FP32 two-lattice pull through the paired kernel, for reference
+    sim32p = Simulation(geom, case.tau, specs, precision="f32", pattern="pull", run_axis=0, nodes_per_lane=2)
+    sec32p = time_steps(sim32p, args.steps, args.warmup, torch)
+    mlups32p = nf * args.steps / sec32p / 1e6 * world
+    del sim32p
 
     # --- stated error: FP16 vs FP64 (FP64 is bit-exact with the CPU oracle) ----
     err_steps = args.err_steps
@@ -243,7 +249,8 @@ def gpu_arm(args, rank, world):
     _, r64, u64 = s64.fields(f=False)
     m64 = s64.monitors()["mass"]
     del s64
-    s16 = Simulation(geom, case.tau, specs, precision="f16s", pattern=args.pattern, run_axis=0, staging=args.staging)
+    s16 = Simulation(geom, case.tau, specs, precision="f16s", pattern=args.pattern, run_axis=0, staging=args.staging,
+                     nodes_per_lane=args.nodes_per_lane)
     m0 = s16.monitors()["mass"]
     s16.step(err_steps, graph=True)
     _, r16, u16 = s16.fields(f=False)
@@ -260,7 +267,7 @@ def gpu_arm(args, rank, world):
     t0 = time.time()
     g2 = case.geometry()
     s2 = Simulation(g2, case.tau, case.boundary_specs(g2), precision="f16s", pattern=args.pattern, run_axis=0,
-                    staging=args.staging)
+                    staging=args.staging, nodes_per_lane=args.nodes_per_lane)
     s2.step(e2e_steps, graph=True)
     _, rho_h, u_h = s2.fields(f=False)
     torch.cuda.synchronize()
@@ -300,9 +307,13 @@ def gpu_arm(args, rank, world):
         "vs_baseline": None, "dtype": "f16-shifted storage, f32 math", "data": "synthetic",
         "config": {"workload": WORKLOAD, "grid": [512, 1024, 512], "fluid_nodes": nf, "triangles": len(case.triangles),
                    "precision": "f16s", "pattern": args.pattern, "run_axis": info16.run_axis,
-                   "staging": "tma" if args.staging == 0 else "direct", "chunks": info16.n_chunks,
+                   "kernel": ("paired: 2 nodes/lane, f32x2 math" if info16.nodes_per_lane == 2 else
+                              "1 node/lane, " + ("tma-staged" if args.staging == 0 else "direct loads")),
+                   "warps_per_block": info16.warps_per_block, "chunks": info16.n_chunks,
                    "l2": "populations exceed L2 (no flush needed)", "parallelism": f"replicas x{world}"},
         "fp32_pull_mlups": mlups32, "f16_over_f32": mlups16 / mlups32,
+        "fp32_pull_plain": "FP32 storage and math, two-lattice pull, one node per lane, direct loads",
+        "fp32_pull_paired_mlups": mlups32p,
         "error_vs_fp64": {"steps": err_steps, "u_rel_l2": u_l2, "u_rel_max": u_max, "rho_max_abs": rho_drift,
                           "mass_change_per_1000_steps": mass_loss_per_1000},
         "roofline": roof, "cpu_baseline": cpu,
@@ -324,6 +335,7 @@ def main():
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--pattern", default="aa", choices=["aa", "pull"])
     ap.add_argument("--staging", type=int, default=1, help="0 = TMA-staged pipeline, 1 = direct loads")
+    ap.add_argument("--nodes-per-lane", type=int, default=0, help="0 = engine default (paired), 1 or 2")
     ap.add_argument("--err-steps", type=int, default=500)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()

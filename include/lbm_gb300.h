@@ -174,8 +174,21 @@ typedef enum lbm_bc_kind {
     LBM_BC_PRESS_POSX = 4,      /* ApplyOutletBc lists 3-5, Simulation.cpp:1093-1279: unknowns +x
                                    (keeps the reference's f10 in place of f16 in Nxz) */
     LBM_BC_PRESS_POSZ = 5,      /* ApplyOutletBc list 6, Simulation.cpp:1290-1346: unknowns +z */
-    LBM_BC_VEL_POSX = 6         /* Boundary::ApplyBc D3Q27, Boundary.cpp:87-123: unknowns +x (Q=27) */
+    LBM_BC_VEL_POSX = 6,        /* Boundary::ApplyBc D3Q27, Boundary.cpp:87-123: unknowns +x (Q=27) */
+    LBM_BC_VELOCITY = 7,        /* any face, Q=19 or 27: the reference's velocity routine with the
+                                   axes relabelled (face field of lbm_list_bc) */
+    LBM_BC_PRESSURE = 8         /* any face, Q=19 or 27: the reference's pressure routine with the
+                                   axes relabelled; for D3Q27, which has no pressure routine in
+                                   the reference, its velocity routine's coefficients */
 } lbm_bc_kind;
+
+/* Face of the LBM_BC_VELOCITY / LBM_BC_PRESSURE kinds: the unknown populations
+ * are those with c along this signed axis (the inlet at the top of a vessel
+ * running along -y has unknowns -y: LBM_FACE_NEGY). */
+typedef enum lbm_face {
+    LBM_FACE_POSX = 0, LBM_FACE_NEGX = 1, LBM_FACE_POSY = 2,
+    LBM_FACE_NEGY = 3, LBM_FACE_POSZ = 4, LBM_FACE_NEGZ = 5
+} lbm_face;
 
 /* Per-list boundary setting.  Velocity lists: the velocity of list node m at
  * step t is (amp[t mod amp_len] * profile[m]) * dir, computed in FP64
@@ -190,6 +203,8 @@ typedef struct lbm_list_bc {
     size_t profile_len;
     const double* amp;         /* amplitude per step (periodic), or NULL */
     size_t amp_len;
+    int32_t face;              /* lbm_face, for LBM_BC_VELOCITY and LBM_BC_PRESSURE */
+    int32_t reserved;
 } lbm_list_bc;
 
 typedef struct lbm_sim_params {
@@ -199,7 +214,7 @@ typedef struct lbm_sim_params {
     double tau;                /* relaxation time; omega = 1/tau (Simulation.cpp:11) */
     const lbm_list_bc* bcs;
     size_t nbcs;
-    int32_t warps_per_block;   /* 1..8; 0 = default / autotuned */
+    int32_t warps_per_block;   /* 1..8; 0 = default (4, or 1 for nodes_per_lane 2) */
     int32_t run_axis;          /* node numbering axis (chunks are runs along it):
                                   1 = y, 2 = z (the reference's x-major order),
                                   0 = the one giving fewer chunks */
@@ -207,8 +222,18 @@ typedef struct lbm_sim_params {
     int32_t nodes_per_lane;    /* 1 = one node per lane (staging applies);
                                   2 = two adjacent nodes per lane with packed
                                       FP32 arithmetic (FP32 and 16-bit storage,
-                                      direct loads); 0 = default (1) */
+                                      direct loads); 0 = default: 2 for FP32
+                                      and 16-bit storage, 1 for FP64 */
+    int32_t corrections;       /* 0 = the reference's behaviour (parity mode); bits:
+                                  LBM_FIX_BB_ALL_DIRS: bounce back every moving direction
+                                    (the reference skips direction 0, Simulation.cpp:1361);
+                                  LBM_FIX_LIST_NODES: bounce back the missing populations of
+                                    inlet/outlet nodes before their Zou-He routine (the
+                                    reference leaves them at their initial value) */
 } lbm_sim_params;
+
+#define LBM_FIX_BB_ALL_DIRS 1
+#define LBM_FIX_LIST_NODES 2
 
 typedef struct lbm_sim lbm_sim;
 
@@ -243,6 +268,20 @@ typedef struct lbm_sim_info {
     int32_t reserved;
 } lbm_sim_info;
 lbm_status lbm_sim_info_get(const lbm_sim* s, lbm_sim_info* info);
+
+/* Autotuner: times every step-kernel variant the handle can run -- one node
+ * per lane with direct loads or TMA staging, two nodes per lane (FP32 and
+ * 16-bit storage), each with 1, 2, 4 and 8 warps per block -- for `launches`
+ * launches on a scratch copy of the state (the simulation does not advance),
+ * and keeps the fastest for later steps.  entries (may be NULL) receives up
+ * to cap results, *n (may be NULL) their number.  Needs device memory for one
+ * more copy of the populations (LBM_ERR_NOMEM otherwise, nothing changed). */
+typedef struct lbm_tune_entry {
+    int32_t nodes_per_lane, staging, warps_per_block, chosen;
+    double ms_per_launch;
+} lbm_tune_entry;
+lbm_status lbm_sim_autotune(lbm_sim* s, int32_t launches, void* stream, lbm_tune_entry* entries, size_t cap,
+                            size_t* n);
 
 /* Host copies of the current post-boundary state f_n (the reference's
  * m_distributions after n iterations) and of rho, u computed from it with the

@@ -312,6 +312,8 @@ enum {
     ORC_BC_PRESS_POSX = 4,      // outlet lists 3-5, Simulation.cpp:1093-1279 (unknowns +x, f10 in Nxz)
     ORC_BC_PRESS_POSZ = 5,      // outlet list 6, Simulation.cpp:1290-1346 (unknowns +z)
     ORC_BC_VEL_POSX_Q27 = 6,    // Boundary::ApplyBc D3Q27, Boundary.cpp:87-123 (unknowns +x)
+    ORC_BC_FACE_VEL = 7,        // any face: the velocity routines above with the axes relabelled
+    ORC_BC_FACE_PRESS = 8,      // any face: the pressure routines above with the axes relabelled
 };
 
 struct OrcSim {
@@ -326,6 +328,8 @@ struct OrcSim {
     std::vector<std::vector<int32_t>> lists;
     std::vector<int> kinds;
     std::vector<double> list_rho;                 // outlet density per list
+    std::vector<int> list_face;                   // face of ORC_BC_FACE_* lists (0..5 = +x,-x,+y,-y,+z,-z unknowns)
+    int corr;                                     // corrections: 1 bounce back every direction, 2 list nodes too
     std::vector<std::vector<double>> list_vel;    // inlet velocity per node (3 per node)
     std::vector<int32_t> wall;                    // wall node ids
     int64_t zero_hits;                            // times the streaming "f != 0" test fired
@@ -348,6 +352,8 @@ void* orc_sim_create(int Q, const int dims[3], const int8_t* role, int nlists, c
     s->lists.resize(nlists);
     s->kinds.assign(kinds, kinds + nlists);
     s->list_rho.assign(list_rho, list_rho + nlists);
+    s->list_face.assign(nlists, 0);
+    s->corr = 0;
     for (size_t p = 0; p < P; ++p) {
         if (role[p] < 0) continue;
         s->grid[p] = (int32_t)n;
@@ -388,6 +394,14 @@ void orc_sim_destroy(void* h) { delete (OrcSim*)h; }
 int64_t orc_sim_nodes(void* h) { return ((OrcSim*)h)->N; }
 int64_t orc_sim_list_size(void* h, int l) { return (int64_t)((OrcSim*)h)->lists[l].size(); }
 int64_t orc_sim_zero_hits(void* h) { return ((OrcSim*)h)->zero_hits; }
+
+void orc_sim_set_face(void* h, int l, int face) { ((OrcSim*)h)->list_face[l] = face; }
+
+// Corrections of the reference's boundary handling (off by default = parity):
+// bit 0 bounces back every moving direction (the reference's ApplyWallBc
+// starts at direction 1, Simulation.cpp:1361), bit 1 also bounces back the
+// missing populations of inlet/outlet nodes, before their Zou-He routine.
+void orc_sim_set_corrections(void* h, int corr) { ((OrcSim*)h)->corr = corr; }
 
 // Sets the inlet velocity of every node of list l (3 doubles per node, list order).
 void orc_sim_set_velocity(void* h, int l, const double* uvw) {
@@ -529,32 +543,100 @@ static void bc_press(double* f, int kind, double rho) {
     }
 }
 
+// Zou-He on an axis-aligned face of any orientation.  The reference writes
+// one routine per orientation (D3Q19: unknowns -y velocity, Boundary.cpp:
+// 129-148; -y/+y/+x/+z pressure, Simulation.cpp:952-1348; D3Q27: +x velocity,
+// Boundary.cpp:87-123); all share one form, restated here over the lattice
+// tables for unknowns sg along axis A (face = 2A + (sg < 0)):
+//   S0 = sum of f over c_A = 0, Sk = sum of f over c_A = -sg
+//   velocity: rho = (S0 + 2 Sk) / (1 - sg u_A)
+//   pressure: u_A = sg (1 - (S0 + 2 Sk) / rho), transverse u = 0
+//   N_T = a sum_{c_A = 0} c_T f - b rho u_T  (a, b = 1/2, 1/3 for D3Q19 and
+//         1/6, 1/9 for D3Q27, the reference's coefficients)
+//   unknown f_q (c_A(q) = sg) = f_opp(q) + 6 w_q rho (c_q . u) - sum_T c_T(q) N_T
+// (the f10 term of outlets 3-5, Simulation.cpp:1124-1129, is the reference's
+// own and stays with ORC_BC_PRESS_POSX).
+static void bc_face(int Q, double* f, int face, bool vel, const double* v, double rho_in) {
+    const int (*C)[3] = Q == 19 ? C19 : C27;
+    const int* opp = Q == 19 ? OPP19 : OPP27;
+    const int A = face >> 1, sg = (face & 1) ? -1 : 1;
+    double S0 = 0.0, Sk = 0.0;
+    for (int q = 0; q < Q; ++q) {
+        if (C[q][A] == 0) S0 += f[q];
+        else if (C[q][A] == -sg) Sk += f[q];
+    }
+    double u[3] = {0.0, 0.0, 0.0}, rho;
+    if (vel) {
+        u[0] = v[0]; u[1] = v[1]; u[2] = v[2];
+        rho = (S0 + 2.0 * Sk) / (1.0 - sg * u[A]);
+    } else {
+        rho = rho_in;
+        u[A] = sg * (1.0 - (S0 + 2.0 * Sk) / rho);
+    }
+    const double a = Q == 19 ? 0.5 : 1.0 / 6.0, b = Q == 19 ? 1.0 / 3.0 : 1.0 / 9.0;
+    double N[3] = {0.0, 0.0, 0.0};
+    for (int t = 0; t < 3; ++t) {
+        if (t == A) continue;
+        double m = 0.0;
+        for (int q = 0; q < Q; ++q)
+            if (C[q][A] == 0 && C[q][t] != 0) m += C[q][t] > 0 ? f[q] : -f[q];
+        N[t] = a * m - b * rho * u[t];
+    }
+    for (int q = 0; q < Q; ++q) {
+        if (C[q][A] != sg) continue;
+        double cu = C[q][0] * u[0] + C[q][1] * u[1] + C[q][2] * u[2];
+        double v2 = f[opp[q]] + 6.0 * weight(Q, q) * rho * cu;
+        for (int t = 0; t < 3; ++t)
+            if (t != A && C[q][t] != 0) v2 -= C[q][t] * N[t];
+        f[q] = v2;
+    }
+}
+
+// One node, any kind (tests): f (Q values) updated in place.
+void orc_zou_he(int Q, int kind, int face, double* f, const double* v, double rho) {
+    if (kind == ORC_BC_VEL_NEGY) bc_vel_negy(f, v);
+    else if (kind == ORC_BC_VEL_POSX_Q27) bc_vel_posx_q27(f, v);
+    else if (kind == ORC_BC_FACE_VEL) bc_face(Q, f, face, true, v, 0.0);
+    else if (kind == ORC_BC_FACE_PRESS) bc_face(Q, f, face, false, nullptr, rho);
+    else bc_press(f, kind, rho);
+}
+
 // One Iterate() body (Simulation.cpp:909-915): Collision, Streaming,
 // ApplyZouHeBc (velocity lists), ApplyWallBc, ApplyOutletBc (pressure lists).
 void orc_sim_step(void* h, int nsteps) {
     OrcSim* s = (OrcSim*)h;
     const int Q = s->Q;
     const int* opp = Q == 19 ? OPP19 : OPP27;
+    const int d0 = (s->corr & 1) ? 0 : 1;
+    auto bounce = [&](int32_t n) {
+        for (int d = d0; d < Q; ++d)
+            if (s->nbr[(size_t)n * Q + d] < 0) s->f[(size_t)n * Q + opp[d]] = s->fnew[(size_t)n * Q + d];
+    };
     for (int it = 0; it < nsteps; ++it) {
         collide(s);
         stream(s);
+        if (s->corr & 2)
+            for (size_t l = 0; l < s->lists.size(); ++l)
+                for (int32_t n : s->lists[l]) bounce(n);
         for (size_t l = 0; l < s->lists.size(); ++l) {
             int k = s->kinds[l];
-            if (k != ORC_BC_VEL_NEGY && k != ORC_BC_VEL_POSX_Q27) continue;
+            if (k != ORC_BC_VEL_NEGY && k != ORC_BC_VEL_POSX_Q27 && k != ORC_BC_FACE_VEL) continue;
             for (size_t m = 0; m < s->lists[l].size(); ++m) {
                 double* f = &s->f[(size_t)s->lists[l][m] * Q];
                 if (k == ORC_BC_VEL_NEGY) bc_vel_negy(f, &s->list_vel[l][3 * m]);
-                else bc_vel_posx_q27(f, &s->list_vel[l][3 * m]);
+                else if (k == ORC_BC_VEL_POSX_Q27) bc_vel_posx_q27(f, &s->list_vel[l][3 * m]);
+                else bc_face(Q, f, s->list_face[l], true, &s->list_vel[l][3 * m], 0.0);
             }
         }
 #pragma omp parallel for schedule(static)
-        for (size_t m = 0; m < s->wall.size(); ++m) {
-            int32_t n = s->wall[m];
-            for (int d = 1; d < Q; ++d)
-                if (s->nbr[(size_t)n * Q + d] < 0) s->f[(size_t)n * Q + opp[d]] = s->fnew[(size_t)n * Q + d];
-        }
+        for (size_t m = 0; m < s->wall.size(); ++m) bounce(s->wall[m]);
         for (size_t l = 0; l < s->lists.size(); ++l) {
             int k = s->kinds[l];
+            if (k == ORC_BC_FACE_PRESS) {
+                for (size_t m = 0; m < s->lists[l].size(); ++m)
+                    bc_face(Q, &s->f[(size_t)s->lists[l][m] * Q], s->list_face[l], false, nullptr, s->list_rho[l]);
+                continue;
+            }
             if (k < ORC_BC_PRESS_NEGY || k > ORC_BC_PRESS_POSZ) continue;
             for (size_t m = 0; m < s->lists[l].size(); ++m)
                 bc_press(&s->f[(size_t)s->lists[l][m] * Q], k, s->list_rho[l]);

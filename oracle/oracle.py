@@ -23,6 +23,9 @@ REF_BIN = {19: os.path.join(HERE, "_ref", "pv2013_ref"), 27: os.path.join(HERE, 
 
 # boundary kinds shared with the engine's lbm_bc_kind numbering
 BC_NONE, BC_VEL_NEGY, BC_PRESS_NEGY, BC_PRESS_POSY, BC_PRESS_POSX, BC_PRESS_POSZ, BC_VEL_POSX = range(7)
+BC_FACE_VEL, BC_FACE_PRESS = 7, 8
+# face of the generic kinds: unknown populations along +x, -x, +y, -y, +z, -z
+FACE_POSX, FACE_NEGX, FACE_POSY, FACE_NEGY, FACE_POSZ, FACE_NEGZ = range(6)
 
 _lib = None
 
@@ -67,6 +70,9 @@ def lib():
         L.orc_sim_zero_hits.restype = C.c_int64
         L.orc_sim_zero_hits.argtypes = [C.c_void_p]
         L.orc_sim_set_velocity.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+        L.orc_sim_set_face.argtypes = [C.c_void_p, C.c_int, C.c_int]
+        L.orc_sim_set_corrections.argtypes = [C.c_void_p, C.c_int]
+        L.orc_zou_he.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_double]
         L.orc_sim_step.argtypes = [C.c_void_p, C.c_int]
         L.orc_sim_get.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.orc_sim_set_f.argtypes = [C.c_void_p, C.c_void_p]
@@ -226,6 +232,12 @@ class OracleSim:
         uvw = np.ascontiguousarray(uvw, dtype=np.float64)
         self.L.orc_sim_set_velocity(self.h, l, _p(uvw))
 
+    def set_corrections(self, corr):
+        self.L.orc_sim_set_corrections(self.h, int(corr))
+
+    def set_face(self, l, face):
+        self.L.orc_sim_set_face(self.h, int(l), int(face))
+
     def step(self, n=1):
         self.L.orc_sim_step(self.h, int(n))
 
@@ -236,6 +248,14 @@ class OracleSim:
         out = np.empty((self.n, self.Q))
         self.L.orc_sim_get(self.h, _p(out), None, None)
         return out
+
+
+def zou_he(Q, kind, f, v=(0.0, 0.0, 0.0), rho=1.0, face=0):
+    """One node's populations after a Zou-He routine (a copy)."""
+    g = np.array(f, dtype=np.float64)
+    vv = np.asarray(v, dtype=np.float64)
+    lib().orc_zou_he(Q, kind, face, _p(g), _p(vv), float(rho))
+    return g
 
 
 def macro(f, Q=19):
@@ -263,21 +283,30 @@ def sum_seq(f, idx):
     return s
 
 
-def run_case(Q, geo, tau, bcs, steps, profile=None, amp=None, inlet_list=0, inlet_dir=(0.0, -1.0, 0.0)):
-    """Runs the restatement on a geometry() result.  bcs: dict list_id -> (kind, rho)."""
+def run_case(Q, geo, tau, bcs, steps, profile=None, amp=None, inlet_list=0, inlet_dir=(0.0, -1.0, 0.0),
+             corrections=0):
+    """Runs the restatement on a geometry() result.  bcs: dict list_id -> (kind, rho)
+    or (kind, rho, face) for the generic face kinds."""
     nl = 64
     kinds = np.zeros(nl, dtype=np.int32)
     rho = np.ones(nl)
-    for l, (k, r) in bcs.items():
-        kinds[l] = k
-        rho[l] = r
+    faces = {}
+    for l, spec in bcs.items():
+        kinds[l] = spec[0]
+        rho[l] = spec[1]
+        if len(spec) > 2:
+            faces[l] = spec[2]
     sim = OracleSim(Q, geo["dims"], geo["role"], kinds, rho, tau)
+    for l, fc in faces.items():
+        sim.set_face(l, fc)
+    if corrections:
+        sim.set_corrections(corrections)
     ninl = sim.list_size(inlet_list)
     prof = np.ones(ninl) if profile is None else np.asarray(profile, dtype=np.float64)
     ampt = np.array([1.0]) if amp is None else np.asarray(amp, dtype=np.float64)
     d = np.asarray(inlet_dir, dtype=np.float64)
     for t in range(steps):
-        if kinds[inlet_list] in (BC_VEL_NEGY, BC_VEL_POSX):
+        if kinds[inlet_list] in (BC_VEL_NEGY, BC_VEL_POSX, BC_FACE_VEL):
             s = ampt[t % len(ampt)] * prof
             sim.set_velocity(inlet_list, np.stack([s * d[0], s * d[1], s * d[2]], axis=1).reshape(-1))
         sim.step(1)

@@ -23,8 +23,12 @@ F64, F32, F16S, BF16S = 0, 1, 2, 3
 PULL, AA, AUTO = 0, 1, 2
 # lbm_bc_kind
 BC_NONE, BC_VEL_NEGY, BC_PRESS_NEGY, BC_PRESS_POSY, BC_PRESS_POSX, BC_PRESS_POSZ, BC_VEL_POSX = range(7)
+BC_VELOCITY, BC_PRESSURE = 7, 8
+# lbm_face
+FACE_POSX, FACE_NEGX, FACE_POSY, FACE_NEGY, FACE_POSZ, FACE_NEGZ = range(6)
 LIST_BOUNDARY, LIST_WALL = -1, -2
 STEP_GRAPH, STEP_MONITOR = 1, 2
+FIX_BB_ALL_DIRS, FIX_LIST_NODES = 1, 2
 
 
 class LbmError(RuntimeError):
@@ -58,13 +62,20 @@ class GeometryInfo(C.Structure):
 class ListBC(C.Structure):
     _fields_ = [("list_id", C.c_int32), ("kind", C.c_int32), ("rho", C.c_double), ("dir", C.c_double * 3),
                 ("profile", C.POINTER(C.c_double)), ("profile_len", C.c_size_t),
-                ("amp", C.POINTER(C.c_double)), ("amp_len", C.c_size_t)]
+                ("amp", C.POINTER(C.c_double)), ("amp_len", C.c_size_t), ("face", C.c_int32),
+                ("reserved", C.c_int32)]
 
 
 class SimParams(C.Structure):
     _fields_ = [("Q", C.c_int32), ("precision", C.c_int32), ("pattern", C.c_int32), ("tau", C.c_double),
                 ("bcs", C.POINTER(ListBC)), ("nbcs", C.c_size_t), ("warps_per_block", C.c_int32),
-                ("run_axis", C.c_int32), ("staging", C.c_int32), ("nodes_per_lane", C.c_int32)]
+                ("run_axis", C.c_int32), ("staging", C.c_int32), ("nodes_per_lane", C.c_int32),
+                ("corrections", C.c_int32)]
+
+
+class TuneEntry(C.Structure):
+    _fields_ = [("nodes_per_lane", C.c_int32), ("staging", C.c_int32), ("warps_per_block", C.c_int32),
+                ("chosen", C.c_int32), ("ms_per_launch", C.c_double)]
 
 
 class SimInfo(C.Structure):
@@ -103,6 +114,7 @@ PROTOTYPES = {
     "lbm_sim_info_get": (C.c_int, [C.c_void_p, _P(SimInfo)]),
     "lbm_sim_fields": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
     "lbm_sim_fields_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
+    "lbm_sim_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
     "lbm_sim_nodes": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "lbm_sim_instance_offsets": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "lbm_sim_monitors": (C.c_int, [C.c_void_p, _P(Monitors), C.c_void_p]),

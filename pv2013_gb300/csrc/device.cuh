@@ -114,7 +114,7 @@ struct ListParam {
     int64_t amp_off;   // offset into the amplitude table array
     int64_t amp_len;   // period of the amplitude table (>= 1)
     int32_t kind;
-    int32_t pad;
+    int32_t face;      // lbm_face of the LBM_BC_VELOCITY / LBM_BC_PRESSURE kinds
 };
 
 // Per-instance parameters.
@@ -154,6 +154,7 @@ struct StepArgs {
     double* out_u;
     const int32_t* out_pos;   // output position of each node (x-major rank of the fluid point)
     int64_t n_nodes;
+    uint32_t corr;            // lbm_sim_params.corrections (LBM_FIX_* bits)
 };
 
 }  // namespace lbm

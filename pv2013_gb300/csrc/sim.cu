@@ -468,10 +468,12 @@ int store_bytes(int s) { return s == ST_F64 ? 8 : (s == ST_F32 ? 4 : 2); }
 // ---------------------------------------------------------------------------
 
 constexpr int64_t kLatticeSlack = 8;   // even: node ids keep the parity of their level
+constexpr int kDryWarps = 4;           // warps per block of snapshot / monitor launches
 
 struct lbm_sim {
     int dev = 0;
     int Q = 19, store = ST_F64, pattern = LBM_PULL, wpb = 4, ra = 2, staging = 0, npl = 1;
+    uint32_t corr = 0;             // LBM_FIX_* bits
     int32_t* err = nullptr;        // device flag: a bounded wait in the step kernel gave up
     int64_t N = 0, nchunks = 0, stride = 0, nz = 0;
     int64_t n_inst = 0;
@@ -733,6 +735,7 @@ lbm_status sim_launch(lbm_sim* S, int mode, bool dry, void* src, void* dst, int6
     a.step = step; a.step_base = step_base;
     a.out_f = of; a.out_rho = orho; a.out_u = ou; a.out_pos = S->out_pos; a.n_nodes = S->NF;
     a.mmask = S->mmask;
+    a.corr = S->corr;
     if (!dry && S->npl == 2) {
         a.chunks = S->chunks2;
         a.nchunks = S->nchunks2;
@@ -750,11 +753,14 @@ lbm_status sim_launch(lbm_sim* S, int mode, bool dry, void* src, void* dst, int6
             default: return launch_tma_bf16s(S->Q, mode, S->ra, a, S->err, S->wpb, st);
         }
     }
+    // snapshot / monitor launches use a fixed block (their partial sums are
+    // sized for it); steps use the tuned one
+    const int wpb = dry ? kDryWarps : S->wpb;
     switch (S->store) {
-        case ST_F64: return launch_step_f64(S->Q, mode, dry, S->ra, a, part, S->wpb, st);
-        case ST_F32: return launch_step_f32(S->Q, mode, dry, S->ra, a, part, S->wpb, st);
-        case ST_F16S: return launch_step_f16s(S->Q, mode, dry, S->ra, a, part, S->wpb, st);
-        default: return launch_step_bf16s(S->Q, mode, dry, S->ra, a, part, S->wpb, st);
+        case ST_F64: return launch_step_f64(S->Q, mode, dry, S->ra, a, part, wpb, st);
+        case ST_F32: return launch_step_f32(S->Q, mode, dry, S->ra, a, part, wpb, st);
+        case ST_F16S: return launch_step_f16s(S->Q, mode, dry, S->ra, a, part, wpb, st);
+        default: return launch_step_bf16s(S->Q, mode, dry, S->ra, a, part, wpb, st);
     }
 }
 
@@ -836,15 +842,21 @@ lbm_status sim_create(const lbm_geometry* const* g, const lbm_sim_params* p, siz
     if (S->store < 0) return fail(LBM_ERR_ARG, "unknown precision %d", p0.precision);
     S->pattern = p0.pattern == LBM_AUTO ? LBM_AA : p0.pattern;
     if (S->pattern != LBM_PULL && S->pattern != LBM_AA) return fail(LBM_ERR_ARG, "unknown pattern %d", p0.pattern);
-    S->wpb = p0.warps_per_block > 0 ? p0.warps_per_block : 4;
+    // default block: 4 warps for the one-node-per-lane kernels, 1 warp (two
+    // chunks) for the paired kernel (measured on the vascular tree)
+    S->wpb = p0.warps_per_block > 0 ? p0.warps_per_block : 0;
     if (S->wpb > 8) return fail(LBM_ERR_ARG, "warps_per_block must be <= 8");
     if (p0.run_axis != 0 && p0.run_axis != 1 && p0.run_axis != 2) return fail(LBM_ERR_ARG, "run_axis must be 0, 1 or 2");
     if (p0.staging != 0 && p0.staging != 1) return fail(LBM_ERR_ARG, "staging must be 0 or 1");
     S->staging = p0.staging;
     if (p0.nodes_per_lane < 0 || p0.nodes_per_lane > 2) return fail(LBM_ERR_ARG, "nodes_per_lane must be 0, 1 or 2");
-    S->npl = p0.nodes_per_lane == 0 ? 1 : p0.nodes_per_lane;
+    S->npl = p0.nodes_per_lane != 0 ? p0.nodes_per_lane : (S->store == ST_F64 ? 1 : 2);
     if (S->npl == 2 && S->store == ST_F64)
         return fail(LBM_ERR_ARG, "nodes_per_lane = 2 needs FP32 or 16-bit storage (FP64 runs one node per lane)");
+    if (S->wpb == 0) S->wpb = S->npl == 2 ? 1 : 4;
+    if (p0.corrections & ~(LBM_FIX_BB_ALL_DIRS | LBM_FIX_LIST_NODES))
+        return fail(LBM_ERR_ARG, "unknown corrections bits 0x%x", (unsigned)p0.corrections);
+    S->corr = (uint32_t)p0.corrections;
     for (size_t i = 0; i < n; ++i) {
         if (p[i].Q != p0.Q || p[i].precision != p0.precision || p[i].pattern != p0.pattern)
             return fail(LBM_ERR_ARG, "batch members must share Q, precision and pattern");
@@ -877,8 +889,8 @@ lbm_status sim_create(const lbm_geometry* const* g, const lbm_sim_params* p, siz
     S->inst_off.push_back(0);
     for (size_t i = 0; i < n; ++i) {
         builds.emplace_back(new InstBuild());
-        LBM_TRY(build_instance(g[i], &p[i], S->Q, (int32_t)i, S->ra, S->npl, node_off, out_off, (int64_t)zall.size(),
-                               nmask, S->err, st, *builds.back()));
+        LBM_TRY(build_instance(g[i], &p[i], S->Q, (int32_t)i, S->ra, S->store == ST_F64 ? 1 : 2, node_off, out_off,
+                               (int64_t)zall.size(), nmask, S->err, st, *builds.back()));
         const InstBuild& B = *builds.back();
         node_off += B.N;
         out_off += B.NF;
@@ -900,7 +912,7 @@ lbm_status sim_create(const lbm_geometry* const* g, const lbm_sim_params* p, siz
     S->nz = (int64_t)zall.size();
     // concatenate per-instance arrays
     LBM_CUDA(cudaMalloc(&S->chunks, sizeof(Chunk) * std::max<int64_t>(nch, 1)));
-    if (S->npl == 2) LBM_CUDA(cudaMalloc(&S->chunks2, sizeof(Chunk) * std::max<int64_t>(nch2, 1)));
+    if (S->store != ST_F64) LBM_CUDA(cudaMalloc(&S->chunks2, sizeof(Chunk) * std::max<int64_t>(nch2, 1)));
     LBM_CUDA(cudaMalloc(&S->mmask, sizeof(uint32_t) * std::max<int64_t>(nmask, 1)));
     LBM_CUDA(cudaMalloc(&S->node_grid, sizeof(int64_t) * S->NF));
     LBM_CUDA(cudaMalloc(&S->out_pos, sizeof(int32_t) * S->N));
@@ -909,7 +921,7 @@ lbm_status sim_create(const lbm_geometry* const* g, const lbm_sim_params* p, siz
         const InstBuild& B = *builds[i];
         LBM_CUDA(cudaMemcpyAsync(S->chunks + chunk_off[i], B.chunks.p, sizeof(Chunk) * B.nchunks,
                                  cudaMemcpyDeviceToDevice, st));
-        if (S->npl == 2 && B.nchunks2)
+        if (S->store != ST_F64 && B.nchunks2)
             LBM_CUDA(cudaMemcpyAsync(S->chunks2 + chunk2_off[i], B.chunks2.p, sizeof(Chunk) * B.nchunks2,
                                      cudaMemcpyDeviceToDevice, st));
         if (B.nmask)
@@ -953,9 +965,14 @@ lbm_status sim_create(const lbm_geometry* const* g, const lbm_sim_params* p, siz
                 L.amp_len = 1;
                 amp.push_back(1.0);
             }
+            L.face = B.face;
+            if (B.kind < LBM_BC_NONE || B.kind > LBM_BC_PRESSURE) return fail(LBM_ERR_ARG, "bc %zu: unknown kind %d", b, B.kind);
+            if ((B.kind == LBM_BC_VELOCITY || B.kind == LBM_BC_PRESSURE) && (B.face < 0 || B.face > 5))
+                return fail(LBM_ERR_ARG, "bc %zu: face must be 0..5 (lbm_face)", b);
             if (p0.Q == 19 && B.kind == LBM_BC_VEL_POSX) return fail(LBM_ERR_ARG, "LBM_BC_VEL_POSX needs Q=27");
-            if (p0.Q == 27 && B.kind != LBM_BC_VEL_POSX && B.kind != LBM_BC_NONE)
-                return fail(LBM_ERR_ARG, "Q=27 supports the reference's D3Q27 inlet (LBM_BC_VEL_POSX) only");
+            if (p0.Q == 27 && B.kind >= LBM_BC_VEL_NEGY && B.kind <= LBM_BC_PRESS_POSZ)
+                return fail(LBM_ERR_ARG, "bc %zu: the reference's D3Q19 routine %d needs Q=19 (use LBM_BC_VELOCITY / "
+                                         "LBM_BC_PRESSURE with a face)", b, B.kind);
         }
     }
     amp.insert(amp.begin(), 1.0);
@@ -987,7 +1004,7 @@ lbm_status sim_create(const lbm_geometry* const* g, const lbm_sim_params* p, siz
         else k_init_bf16<<<blocks_for(tot, 256), 256, 0, st>>>((__nv_bfloat16*)S->buf[b], tot);
     }
     // monitor buffers (one partial per block of the dry launch)
-    S->part_blocks = std::max<int64_t>((S->nchunks + S->wpb - 1) / S->wpb, 1);
+    S->part_blocks = std::max<int64_t>((S->nchunks + kDryWarps - 1) / kDryWarps, 1);
     LBM_CUDA(cudaMalloc(&S->part, sizeof(double) * 4 * S->part_blocks));
     LBM_CUDA(cudaMalloc(&S->partbad, sizeof(int32_t) * S->part_blocks));
     LBM_CUDA(cudaMalloc(&S->mon, sizeof(MonOut)));
@@ -1086,6 +1103,86 @@ lbm_status lbm_sim_step(lbm_sim* S, int64_t nsteps, uint32_t flags, void* stream
             return fail(LBM_ERR_DIVERGED, "diverged at step %lld: mass %.17g (initial %.17g), non-finite=%d",
                         (long long)S->steps_done, m.mass, S->mass0, m.nonfinite);
     }
+    return LBM_OK;
+}
+
+lbm_status lbm_sim_autotune(lbm_sim* S, int32_t launches, void* stream, lbm_tune_entry* entries, size_t cap,
+                            size_t* n) {
+    if (!S || launches < 2) return fail(LBM_ERR_ARG, "lbm_sim_autotune: null handle or fewer than 2 launches");
+    clear_error();
+    cudaStream_t st = (cudaStream_t)stream;
+    // scratch copy of the state: the candidates run on it, the simulation is untouched
+    const size_t bytes = (size_t)S->stride * S->Q * store_bytes(S->store);
+    const int nb = S->pattern == LBM_PULL ? 2 : 1;
+    void* scratch[2] = {nullptr, nullptr};
+    for (int b = 0; b < nb; ++b)
+        if (cudaMalloc(&scratch[b], bytes) != cudaSuccess) {
+            if (scratch[0]) cudaFree(scratch[0]);
+            cudaGetLastError();
+            return fail(LBM_ERR_NOMEM, "lbm_sim_autotune: no room for a scratch copy of the state (%zu bytes)", bytes);
+        }
+    struct Cand { int npl, staging, wpb; float ms; };
+    std::vector<Cand> cands;
+    const int wpbs[4] = {1, 2, 4, 8};
+    for (int w : wpbs) cands.push_back({1, 1, w, 0.f});
+    for (int w : wpbs) cands.push_back({1, 0, w, 0.f});
+    if (S->store != ST_F64)
+        for (int w : wpbs) cands.push_back({2, 1, w, 0.f});
+    const int save_npl = S->npl, save_staging = S->staging, save_wpb = S->wpb;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    lbm_status res = LBM_OK;
+    auto run = [&](int count, int parity0) -> lbm_status {
+        for (int i = 0; i < count; ++i) {
+            Partials np = {nullptr, nullptr, nullptr, nullptr, nullptr};
+            lbm_status s;
+            if (S->pattern == LBM_PULL)
+                s = sim_launch(S, MODE_PULL, false, scratch[i & 1], scratch[1 - (i & 1)], S->steps_done + i, nullptr,
+                               np, nullptr, nullptr, nullptr, st);
+            else
+                s = sim_launch(S, ((parity0 + i) & 1) ? MODE_AA_ODD : MODE_AA_EVEN, false, scratch[0], scratch[0],
+                               S->steps_done + i, nullptr, np, nullptr, nullptr, nullptr, st);
+            if (s != LBM_OK) return s;
+        }
+        return LBM_OK;
+    };
+    do {
+        if (cudaMemcpyAsync(scratch[0], S->buf[S->pattern == LBM_PULL ? S->cur : 0], bytes, cudaMemcpyDeviceToDevice,
+                            st) != cudaSuccess ||
+            cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+            res = fail(LBM_ERR_CUDA, "lbm_sim_autotune: set-up failed");
+            break;
+        }
+        const int parity0 = (int)(S->steps_done & 1);
+        for (Cand& c : cands) {
+            S->npl = c.npl; S->staging = c.staging; S->wpb = c.wpb;
+            if ((res = run(2, parity0)) != LBM_OK) break;      // warm-up (even count keeps the AA parity)
+            cudaEventRecord(e0, st);
+            if ((res = run(launches & ~1, parity0)) != LBM_OK) break;
+            cudaEventRecord(e1, st);
+            if (cudaEventSynchronize(e1) != cudaSuccess) { res = fail(LBM_ERR_CUDA, "lbm_sim_autotune: timing"); break; }
+            cudaEventElapsedTime(&c.ms, e0, e1);
+            c.ms /= (float)(launches & ~1);
+        }
+    } while (false);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    for (int b = 0; b < nb; ++b) cudaFree(scratch[b]);
+    S->npl = save_npl; S->staging = save_staging; S->wpb = save_wpb;
+    if (res != LBM_OK) return res;
+    LBM_TRY(check_timeout(S, st));
+    const Cand* best = &cands[0];
+    for (const Cand& c : cands) if (c.ms < best->ms) best = &c;
+    S->npl = best->npl; S->staging = best->staging; S->wpb = best->wpb;
+    free_graph(S);                         // the captured launches used the old shape
+    if (n) *n = cands.size();
+    if (entries)
+        for (size_t i = 0; i < cands.size() && i < cap; ++i) {
+            entries[i].nodes_per_lane = cands[i].npl;
+            entries[i].staging = cands[i].staging;
+            entries[i].warps_per_block = cands[i].wpb;
+            entries[i].chosen = &cands[i] == best ? 1 : 0;
+            entries[i].ms_per_launch = cands[i].ms;
+        }
     return LBM_OK;
 }
 

@@ -210,6 +210,83 @@ __device__ __forceinline__ void zh_press(T* f, int kind, T rho) {
     }
 }
 
+// Zou-He on an axis-aligned face of any orientation.  The reference writes
+// one routine per orientation (the functions above); they share one form,
+// written here over the lattice tables for unknowns sg along axis A
+// (face = 2A + (sg < 0)):
+//   S0 = sum of f over c_A = 0, Sk = sum of f over c_A = -sg
+//   velocity: rho = (S0 + 2 Sk) / (1 - sg u_A)
+//   pressure: u_A = sg (1 - (S0 + 2 Sk) / rho), transverse u = 0
+//   N_T = a sum_{c_A = 0} c_T f - b rho u_T  (a, b = 1/2, 1/3 for D3Q19 and
+//         1/6, 1/9 for D3Q27, the reference's coefficients)
+//   unknown f_q (c_A(q) = sg) = f_opp(q) + 6 w_q rho (c_q . u) - sum_T c_T(q) N_T
+template <int Q>
+__host__ __device__ constexpr int lat_c(int q, int ax) {
+    return ax == 0 ? Lat<Q>::cx(q) : (ax == 1 ? Lat<Q>::cy(q) : Lat<Q>::cz(q));
+}
+
+template <int Q, class T>
+__device__ __forceinline__ void zh_face(T* f, int face, bool vel, const T* v, T rho_in) {
+    using L = Lat<Q>;
+    const int A = face >> 1, sg = (face & 1) ? -1 : 1;
+    T S0 = T(0), Sk = T(0);
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const int ca = lat_c<Q>(q, A);
+        if (ca == 0) S0 += f[q];
+        else if (ca == -sg) Sk += f[q];
+    }
+    T u[3] = {T(0), T(0), T(0)};
+    T rho;
+    if (vel) {
+        u[0] = v[0]; u[1] = v[1]; u[2] = v[2];
+        rho = (S0 + T(2) * Sk) / (T(1) - T(sg) * u[A]);
+    } else {
+        rho = rho_in;
+        u[A] = T(sg) * (T(1) - (S0 + T(2) * Sk) / rho);
+    }
+    const T ka = Q == 19 ? T(0.5) : T(1.0) / T(6.0), kb = Q == 19 ? T(1.0) / T(3.0) : T(1.0) / T(9.0);
+    T N[3] = {T(0), T(0), T(0)};
+#pragma unroll
+    for (int t = 0; t < 3; ++t) {
+        if (t == A) continue;
+        T m = T(0);
+#pragma unroll
+        for (int q = 0; q < Q; ++q)
+            if (lat_c<Q>(q, A) == 0 && lat_c<Q>(q, t) != 0) m += lat_c<Q>(q, t) > 0 ? f[q] : -f[q];
+        N[t] = ka * m - kb * rho * u[t];
+    }
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        if (lat_c<Q>(q, A) != sg) continue;
+        const T cu = T(L::cx(q)) * u[0] + T(L::cy(q)) * u[1] + T(L::cz(q)) * u[2];
+        T val = f[L::opp(q)] + T(6.0 * L::w(q)) * rho * cu;
+#pragma unroll
+        for (int t = 0; t < 3; ++t)
+            if (t != A && lat_c<Q>(q, t) != 0) val -= T(lat_c<Q>(q, t)) * N[t];
+        f[q] = val;
+    }
+}
+
+// Any Zou-He kind on plain populations p (velocity v for the velocity kinds).
+template <int Q, class T>
+__device__ __forceinline__ void zou_he_apply(T* p, int kind, int face, const T* v, T rho) {
+    if (kind == LBM_BC_VELOCITY) {
+        zh_face<Q, T>(p, face, true, v, rho);
+    } else if (kind == LBM_BC_PRESSURE) {
+        zh_face<Q, T>(p, face, false, v, rho);
+    } else if constexpr (Q == 19) {
+        if (kind == LBM_BC_VEL_NEGY) zh_vel_negy<T>(p, v);
+        else zh_press<T>(p, kind, rho);
+    } else {
+        if (kind == LBM_BC_VEL_POSX) zh_vel_posx_q27<T>(p, v);
+    }
+}
+
+__host__ __device__ constexpr bool is_velocity_kind(int kind) {
+    return kind == LBM_BC_VEL_NEGY || kind == LBM_BC_VEL_POSX || kind == LBM_BC_VELOCITY;
+}
+
 // rho and u from plain populations with the reference's grouped sums
 // (Simulation.cpp:32-79 for D3Q19, :82-148 for D3Q27).
 template <int Q, class T>
@@ -325,11 +402,14 @@ __device__ __forceinline__ void node_update(const StepArgs& a, int32_t zslot0, t
     const void* A = a.src;
     if (__any_sync(__activemask(), missing != 0u)) {
         // predicated per population, so lanes of a warp do not diverge
-        const bool wall = (wmask >> lane) & 1u;
+        // wall nodes bounce back (inlet/outlet nodes too with LBM_FIX_LIST_NODES);
+        // the reference never bounces back population opp(0) of D3Q19
+        const bool wall = ((wmask >> lane) & 1u) || (a.corr & LBM_FIX_LIST_NODES);
+        const bool all_dirs = a.corr & LBM_FIX_BB_ALL_DIRS;
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
             const bool miss = (missing >> q) & 1u;
-            const bool bb = miss && wall && q != L::NO_BB_POP;
+            const bool bb = miss && wall && (q != L::NO_BB_POP || all_dirs);
             if constexpr (MODE == MODE_PULL) {
                 if (bb) f[q] = ld<S, Q, true>(A, a.stride, L::opp(q), n);
             } else if constexpr (MODE == MODE_AA_ODD) {
@@ -351,21 +431,17 @@ __device__ __forceinline__ void node_update(const StepArgs& a, int32_t zslot0, t
         T p[Q];
 #pragma unroll
         for (int q = 0; q < Q; ++q) p[q] = plain<S, Q>(f[q], q);
-        if (z.kind == LBM_BC_VEL_NEGY || z.kind == LBM_BC_VEL_POSX) {
+        T v[3] = {T(0), T(0), T(0)};
+        if (is_velocity_kind(z.kind)) {
             // 32-bit phase: the step count stays below 2^32 (lbm_sim_step checks)
             const double amp = a.amp[lp.amp_off + (uint32_t)(step - 1) % (uint32_t)lp.amp_len];
             const double sc = amp * z.profile;
-            const T v[3] = {T(sc * lp.dir[0]), T(sc * lp.dir[1]), T(sc * lp.dir[2])};
-            if constexpr (Q == 19) {
-                if (z.kind == LBM_BC_VEL_NEGY) zh_vel_negy<T>(p, v);
-            } else {
-                if (z.kind == LBM_BC_VEL_POSX) zh_vel_posx_q27<T>(p, v);
-            }
+            v[0] = T(sc * lp.dir[0]); v[1] = T(sc * lp.dir[1]); v[2] = T(sc * lp.dir[2]);
             zdir = 1.0;
         } else {
-            if constexpr (Q == 19) zh_press<T>(p, z.kind, T(lp.rho));
             zdir = -1.0;
         }
+        zou_he_apply<Q, T>(p, z.kind, lp.face, v, T(lp.rho));
 #pragma unroll
         for (int q = 0; q < Q; ++q) f[q] = unplain<S, Q>(p[q], q);
     }

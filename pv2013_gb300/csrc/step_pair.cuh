@@ -63,9 +63,14 @@ template <> struct PairWord<ST_F32> { using W = uint2; };
 template <> struct PairWord<ST_F16S> { using W = uint32_t; };
 template <> struct PairWord<ST_BF16S> { using W = uint32_t; };
 
+template <int S> constexpr int elem_bytes() { return S == ST_F32 ? 4 : 2; }
+
+// the pair word holding elements off and off+1 (off even: a population
+// plane's offset plus an even node id) -- one base pointer and 32-bit element
+// offsets keep the address arithmetic in 32-bit registers
 template <int S>
 __device__ __forceinline__ typename PairWord<S>::W ldw(const void* base, uint32_t off) {
-    return ((const typename PairWord<S>::W*)base)[off >> 1];
+    return reinterpret_cast<const typename PairWord<S>::W*>(base)[off >> 1];
 }
 // high element of word a, low element of word b (a pair one level out of phase)
 template <int S>
@@ -105,14 +110,14 @@ __device__ __forceinline__ typename PairWord<S>::W pack(F2 v, int q) {
 }
 template <int S>
 __device__ __forceinline__ void stw(void* base, uint32_t off, typename PairWord<S>::W w) {
-    ((typename PairWord<S>::W*)base)[off >> 1] = w;
+    reinterpret_cast<typename PairWord<S>::W*>(base)[off >> 1] = w;
 }
-// one element (one node) of a pair
+// one element (one node) of a plane
 template <int S, int Q>
 __device__ __forceinline__ void st_one(void* base, uint32_t off, float v, int q) {
-    if constexpr (S == ST_F32) ((float*)base)[off] = v + (float)Lat<Q>::w(q);
-    else if constexpr (S == ST_F16S) ((__half*)base)[off] = __float2half_rn(v);
-    else ((__nv_bfloat16*)base)[off] = __float2bfloat16_rn(v);
+    if constexpr (S == ST_F32) reinterpret_cast<float*>(base)[off] = v + (float)Lat<Q>::w(q);
+    else if constexpr (S == ST_F16S) reinterpret_cast<__half*>(base)[off] = __float2half_rn(v);
+    else reinterpret_cast<__nv_bfloat16*>(base)[off] = __float2bfloat16_rn(v);
 }
 
 // ---------------------------------------------------------------------------
@@ -174,19 +179,14 @@ __device__ __forceinline__ void zou_he_half(const StepArgs& a, int slot, typenam
     T p[Q];
 #pragma unroll
     for (int q = 0; q < Q; ++q) p[q] = half_plain<S, Q>(raw[q * 32], hi, q);
-    if (z.kind == LBM_BC_VEL_NEGY || z.kind == LBM_BC_VEL_POSX) {
+    T v[3] = {T(0), T(0), T(0)};
+    if (is_velocity_kind(z.kind)) {
         // 32-bit phase: the step count stays below 2^32 (lbm_sim_step checks)
-            const double amp = a.amp[lp.amp_off + (uint32_t)(step - 1) % (uint32_t)lp.amp_len];
+        const double amp = a.amp[lp.amp_off + (uint32_t)(step - 1) % (uint32_t)lp.amp_len];
         const double sc = amp * z.profile;
-        const T v[3] = {T(sc * lp.dir[0]), T(sc * lp.dir[1]), T(sc * lp.dir[2])};
-        if constexpr (Q == 19) {
-            if (z.kind == LBM_BC_VEL_NEGY) zh_vel_negy<T>(p, v);
-        } else {
-            if (z.kind == LBM_BC_VEL_POSX) zh_vel_posx_q27<T>(p, v);
-        }
-    } else {
-        if constexpr (Q == 19) zh_press<T>(p, z.kind, T(lp.rho));
+        v[0] = T(sc * lp.dir[0]); v[1] = T(sc * lp.dir[1]); v[2] = T(sc * lp.dir[2]);
     }
+    zou_he_apply<Q, T>(p, z.kind, lp.face, v, T(lp.rho));
 #pragma unroll
     for (int q = 0; q < Q; ++q) raw[q * 32] = set_half_plain<S, Q>(raw[q * 32], hi, p[q], q);
 }
@@ -274,16 +274,19 @@ __global__ void __launch_bounds__(256, PairMinBlocks<Q, S, MODE>::value) k_step2
     const int t = lane & 15;                      // pair index within the chunk
     const int64_t ci = ((int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 2 + (lane >> 4);
     const bool have_chunk = ci < a.nchunks;
-    const Chunk* cp = a.chunks + (have_chunk ? ci : 0);
-    const int32_t n0 = have_chunk ? __ldg(&cp->n0) : 0;
-    const uint32_t li = have_chunk ? __ldg(&cp->len_inst) : 0u;
+    // chunk descriptor words 0-7 (n0, len_inst, wmask, zmask, bmask, zslot0, mslot0, K0)
+    const uint4* cw = reinterpret_cast<const uint4*>(a.chunks + (have_chunk ? ci : 0));
+    const uint4 d0 = have_chunk ? __ldg(cw) : make_uint4(0u, 0u, 0u, 0u);
+    const uint4 d1 = have_chunk ? __ldg(cw + 1) : make_uint4(0u, 0u, 0u, 0u);
+    const int32_t n0 = (int32_t)d0.x;
+    const uint32_t li = d0.y;
     const bool act = have_chunk && 2 * t < (int)(li & 63u);
     // node slots 2t (lo) and 2t+1 (hi) of the chunk
-    const uint32_t bm_all = act ? __ldg(&cp->bmask) : 0u;
-    const uint32_t zm_all = act ? __ldg(&cp->zmask) : 0u;
+    const uint32_t bm_all = act ? d1.x : 0u;
+    const uint32_t zm_all = act ? d0.w : 0u;
     uint32_t m_lo = 0u, m_hi = 0u;
     if ((bm_all >> (2 * t)) & 3u) {
-        const int32_t ms = __ldg(&cp->mslot0) + __popc(bm_all & ((1u << (2 * t)) - 1u));
+        const int32_t ms = (int32_t)d1.z + __popc(bm_all & ((1u << (2 * t)) - 1u));
         if ((bm_all >> (2 * t)) & 1u) m_lo = __ldg(a.mmask + ms);
         if ((bm_all >> (2 * t + 1)) & 1u) m_hi = __ldg(a.mmask + ms + ((bm_all >> (2 * t)) & 1u));
     }
@@ -292,22 +295,37 @@ __global__ void __launch_bounds__(256, PairMinBlocks<Q, S, MODE>::value) k_step2
     const int64_t step = a.step + (a.step_base ? *a.step_base : 0);
     const void* A = a.src;
 
+    // column bases (virtual id of level r0-1) of the eight neighbour columns
+    auto load_K = [&](int32_t* K, bool fresh) {
+        uint4 k1, k2;
+        uint32_t k0;
+        if (fresh) {
+            asm volatile("ld.global.nc.u32 %0, [%1];" : "=r"(k0) : "l"(&cw[1].w));
+            asm volatile("ld.global.nc.v4.u32 {%0, %1, %2, %3}, [%4];"
+                         : "=r"(k1.x), "=r"(k1.y), "=r"(k1.z), "=r"(k1.w) : "l"(cw + 2));
+            asm volatile("ld.global.nc.v4.u32 {%0, %1, %2, %3}, [%4];"
+                         : "=r"(k2.x), "=r"(k2.y), "=r"(k2.z), "=r"(k2.w) : "l"(cw + 3));
+        } else {
+            k0 = d1.w;
+            k1 = __ldg(cw + 2);
+            k2 = __ldg(cw + 3);
+        }
+        K[0] = (int32_t)k0; K[1] = (int32_t)k1.x; K[2] = (int32_t)k1.y; K[3] = (int32_t)k1.z;
+        K[4] = (int32_t)k1.w; K[5] = (int32_t)k2.x; K[6] = (int32_t)k2.y; K[7] = (int32_t)k2.z;
+    };
+
     W raw[Q];
     if (act) {
         int32_t K[8];
-        if constexpr (MODE != MODE_AA_EVEN) {
-#pragma unroll
-            for (int c = 0; c < 8; ++c) K[c] = __ldg(&cp->K[c]);
-        }
+        if constexpr (MODE != MODE_AA_EVEN) load_K(K, false);
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
             if constexpr (MODE == MODE_AA_EVEN) {
                 raw[q] = ldw<S>(A, (uint32_t)q * st + e);
             } else {
                 const int da = -X::a(q), db = -X::b(q), o = -X::r(q);
-                const int plane = MODE == MODE_AA_ODD ? L::opp(q) : q;
+                const uint32_t pb = (uint32_t)(MODE == MODE_AA_ODD ? L::opp(q) : q) * st;
                 const uint32_t s = (uint32_t)((da == 0 && db == 0 ? n0 - 1 : K[col8(da, db)]) + 1 + 2 * t);
-                const uint32_t pb = (uint32_t)plane * st;
                 if (o == 0) raw[q] = ldw<S>(A, pb + s);
                 else if (o > 0) raw[q] = straddle<S>(ldw<S>(A, pb + s), ldw<S>(A, pb + s + 2));
                 else raw[q] = straddle<S>(ldw<S>(A, pb + s - 2), ldw<S>(A, pb + s));
@@ -317,18 +335,22 @@ __global__ void __launch_bounds__(256, PairMinBlocks<Q, S, MODE>::value) k_step2
 
     // missing populations (boundary nodes): bounce-back or the initial value
     if (__any_sync(0xffffffffu, (m_lo | m_hi) != 0u)) {
-        const uint32_t wm = act ? (__ldg(&cp->wmask) >> (2 * t)) & 3u : 0u;
+        uint32_t wm = 0u;
+        if (act) asm volatile("ld.global.nc.u32 %0, [%1];" : "=r"(wm) : "l"(&cw[0].z));   // wmask, read late
+        wm = (wm >> (2 * t)) & 3u;
+        if (a.corr & LBM_FIX_LIST_NODES) wm = 3u;       // every boundary node bounces back
+        const bool all_dirs = a.corr & LBM_FIX_BB_ALL_DIRS;
         const bool w_lo = wm & 1u, w_hi = (wm >> 1) & 1u;
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
             const bool ml = (m_lo >> q) & 1u, mh = (m_hi >> q) & 1u;
             if (ml || mh) {
-                const bool bl = ml && w_lo && q != L::NO_BB_POP, bh = mh && w_hi && q != L::NO_BB_POP;
+                const bool dir_ok = q != L::NO_BB_POP || all_dirs;
+                const bool bl = ml && w_lo && dir_ok, bh = mh && w_hi && dir_ok;
                 if constexpr (MODE != MODE_AA_EVEN) {
                     // bounce-back source: own node, slot opp(q) (pull) or slot q (AA odd)
                     if (bl || bh) {
-                        const int plane = MODE == MODE_PULL ? L::opp(q) : q;
-                        const W own = ldw<S>(A, (uint32_t)plane * st + e);
+                        const W own = ldw<S>(A, (uint32_t)(MODE == MODE_PULL ? L::opp(q) : q) * st + e);
                         if (bl) raw[q] = take_half<S>(raw[q], false, own);
                         if (bh) raw[q] = take_half<S>(raw[q], true, own);
                     }
@@ -348,7 +370,9 @@ __global__ void __launch_bounds__(256, PairMinBlocks<Q, S, MODE>::value) k_step2
 #pragma unroll
         for (int q = 0; q < Q; ++q) buf[q * 32] = raw[q];
         if (step > 0 && zm) {
-            const int z0 = __ldg(&cp->zslot0) + __popc(zm_all & ((1u << (2 * t)) - 1u));
+            int32_t zs;
+            asm volatile("ld.global.nc.u32 %0, [%1];" : "=r"(zs) : "l"(&cw[1].y));     // zslot0, read late
+            const int z0 = zs + __popc(zm_all & ((1u << (2 * t)) - 1u));
             if (zm & 1u) zou_he_half<Q, S>(a, z0, buf, false, step);
             if (zm & 2u) zou_he_half<Q, S>(a, z0 + (int)(zm & 1u), buf, true, step);
         }
@@ -356,8 +380,8 @@ __global__ void __launch_bounds__(256, PairMinBlocks<Q, S, MODE>::value) k_step2
         for (int q = 0; q < Q; ++q) raw[q] = buf[q * 32];
     }
     if (!act) return;
-    void* D = a.dst;
     const float om = a.insts[li >> 8].omega_f;
+    void* D = a.dst;
     if constexpr (MODE == MODE_PULL) {
         collide2<Q, S>(raw, om, [&](int q, F2 v) { stw<S>(D, (uint32_t)q * st + e, pack<S, Q>(v, q)); });
     } else if constexpr (MODE == MODE_AA_EVEN) {
@@ -365,10 +389,11 @@ __global__ void __launch_bounds__(256, PairMinBlocks<Q, S, MODE>::value) k_step2
     } else {
         // AA odd: f*_q to slot q of x + c_q, or (absent destination) to slot
         // opp(q) of x; ghost slots of the pair store nothing
-        const uint32_t vm = (__ldg(&cp->vmask) >> (2 * t)) & 3u;
+        uint32_t vm;
+        asm volatile("ld.global.nc.u32 %0, [%1];" : "=r"(vm) : "l"(&cw[3].w));
+        vm = (vm >> (2 * t)) & 3u;
         int32_t K[8];
-#pragma unroll
-        for (int c = 0; c < 8; ++c) K[c] = ld_fresh(&cp->K[c]);
+        load_K(K, true);
         collide2<Q, S>(raw, om, [&](int q, F2 v) {
             const int da = X::a(q), db = X::b(q), o = X::r(q);
             const uint32_t s = (uint32_t)((da == 0 && db == 0 ? n0 - 1 : K[col8(da, db)]) + 1 + 2 * t);

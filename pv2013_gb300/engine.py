@@ -239,11 +239,13 @@ class BoundarySpec:
     dir: Sequence[float] = (0.0, -1.0, 0.0)
     profile: Optional[np.ndarray] = None
     amp: Optional[np.ndarray] = None
+    face: int = 0                       # lbm_face, for BC_VELOCITY / BC_PRESSURE
     _keep: list = field(default_factory=list, repr=False)
 
     def to_c(self):
         b = _capi.ListBC()
         b.list_id, b.kind, b.rho = self.list_id, self.kind, float(self.rho)
+        b.face = int(self.face)
         for a in range(3):
             b.dir[a] = float(self.dir[a])
         if self.profile is not None:
@@ -261,7 +263,8 @@ PRECISIONS = {"f64": _capi.F64, "f32": _capi.F32, "f16s": _capi.F16S, "bf16s": _
 PATTERNS = {"pull": _capi.PULL, "aa": _capi.AA, "auto": _capi.AUTO}
 
 
-def _params(Q, precision, pattern, tau, bcs, warps_per_block, run_axis=0, staging=0, nodes_per_lane=0):
+def _params(Q, precision, pattern, tau, bcs, warps_per_block, run_axis=0, staging=0, nodes_per_lane=0,
+            corrections=0):
     cb = [b.to_c() for b in bcs]
     arr = (_capi.ListBC * max(len(cb), 1))(*cb)
     p = _capi.SimParams()
@@ -275,6 +278,7 @@ def _params(Q, precision, pattern, tau, bcs, warps_per_block, run_axis=0, stagin
     p.run_axis = int(run_axis)
     p.staging = int(staging)
     p.nodes_per_lane = int(nodes_per_lane)
+    p.corrections = int(corrections)
     return p, arr
 
 
@@ -286,7 +290,7 @@ class Simulation:
     """
 
     def __init__(self, geometry, tau, bcs=(), Q=19, precision="f64", pattern="pull", warps_per_block=0, run_axis=0,
-                 staging=0, stream=None, nodes_per_lane=0):
+                 staging=0, stream=None, nodes_per_lane=0, corrections=0):
         lib = load()
         self._stream = C.c_void_p(stream) if stream else None
         h = C.c_void_p()
@@ -297,14 +301,16 @@ class Simulation:
             keep = []
             params = (_capi.SimParams * n)()
             for i in range(n):
-                p, arr = _params(Q, precision, pattern, taus[i], bcl[i], warps_per_block, run_axis, staging, nodes_per_lane)
+                p, arr = _params(Q, precision, pattern, taus[i], bcl[i], warps_per_block, run_axis, staging, nodes_per_lane,
+                                 corrections)
                 keep.append((arr, bcl[i]))
                 params[i] = p
             geoms = (C.c_void_p * n)(*[g.handle for g in geometry])
             check(lib.lbm_batch_create(geoms, params, n, self._stream, C.byref(h)))
             self.geometries = list(geometry)
         else:
-            p, arr = _params(Q, precision, pattern, tau, bcs, warps_per_block, run_axis, staging, nodes_per_lane)
+            p, arr = _params(Q, precision, pattern, tau, bcs, warps_per_block, run_axis, staging, nodes_per_lane,
+                             corrections)
             check(lib.lbm_sim_create(geometry.handle, C.byref(p), self._stream, C.byref(h)))
             self.geometries = [geometry]
         self._h = h
@@ -361,6 +367,16 @@ class Simulation:
         check(load().lbm_sim_monitors(self._h, C.byref(m), self._stream))
         return {"step": m.step, "mass": m.mass, "inlet_flux": m.inlet_flux, "outlet_flux": m.outlet_flux,
                 "max_speed": m.max_speed, "nonfinite": bool(m.nonfinite)}
+
+    def autotune(self, launches=20):
+        """Times the step-kernel variants on a scratch copy of the state and
+        keeps the fastest; returns [(nodes_per_lane, staging, warps_per_block,
+        ms_per_launch, chosen)]."""
+        ents = (_capi.TuneEntry * 16)()
+        n = C.c_size_t()
+        check(load().lbm_sim_autotune(self._h, int(launches), self._stream, ents, 16, C.byref(n)))
+        return [(e.nodes_per_lane, e.staging, e.warps_per_block, e.ms_per_launch, bool(e.chosen))
+                for e in ents[:n.value]]
 
     def set_divergence_tolerance(self, tol):
         check(load().lbm_sim_set_divergence_tolerance(self._h, float(tol)))

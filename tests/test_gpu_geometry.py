@@ -45,6 +45,18 @@ def test_bifurcation_matches_oracle(oracle_mod):
     _check_case(oracle_mod, cases.bifurcation(nx=128, ny=256, nz=128, r_parent=12, r_child=9, h=1.3))
 
 
+def test_full_bifurcation_matches_oracle(oracle_mod):
+    """The bifurcation workload at its full size (256 x 512 x 256 grid)."""
+    _check_case(oracle_mod, cases.bifurcation())
+
+
+def test_full_vascular_tree_matches_oracle(oracle_mod):
+    """The benchmark's vascular tree (512 x 1024 x 512 grid, 2.07 M triangles,
+    32 outlet lists): node-type field, boundary points and every list bit-exact
+    with the oracle (about a minute of OpenMP work on the host)."""
+    _check_case(oracle_mod, cases.vascular_tree(h=2.2))
+
+
 def test_fine_spacing_matches_oracle(oracle_mod):
     """Spacing 0.37 (grid coordinates not representable exactly)."""
     O = oracle_mod

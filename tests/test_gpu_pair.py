@@ -127,3 +127,28 @@ def test_pair_kernel_rejects_fp64():
     with pytest.raises(_capi.LbmError) as e:
         Simulation(geom, c.tau, c.boundary_specs(geom), precision="f64", nodes_per_lane=2)
     assert e.value.status == _capi.ERR_ARG
+
+
+@pytest.mark.parametrize("pattern", ["pull", "aa"])
+def test_autotune_keeps_state_and_results(pattern):
+    """The autotuner runs its candidates on a scratch copy: the step count and
+    populations are unchanged by it, and the run it tunes agrees with an
+    untuned run (FP32 rounding)."""
+    c = cases.vessel(4003)
+    geom = c.geometry()
+    a = Simulation(geom, c.tau, c.boundary_specs(geom), precision="f32", pattern=pattern)
+    b = Simulation(geom, c.tau, c.boundary_specs(geom), precision="f32", pattern=pattern)
+    a.step(5)
+    b.step(5)
+    f_before = b.fields()[0]
+    res = b.autotune(launches=6)
+    assert len(res) == 12 and sum(r[4] for r in res) == 1
+    assert all(r[3] > 0 for r in res)
+    assert b.info().steps_done == 5
+    assert np.array_equal(b.fields()[0], f_before)
+    chosen = [r for r in res if r[4]][0]
+    info = b.info()
+    assert (info.nodes_per_lane, info.warps_per_block) == (chosen[0], chosen[2])
+    a.step(40, graph=True)
+    b.step(40, graph=True)
+    assert rel_l2(b.fields()[0], a.fields()[0]) < 1e-6

@@ -186,3 +186,35 @@ def test_d3q27_fp64_bit_exact(oracle_mod):
         ref = O.run_case(27, geo, c.tau, {0: (O.BC_VEL_POSX, 1.0)}, 11, profile=prof, amp=c.amp_table(),
                          inlet_dir=(1.0, 0.0, 0.0))
         assert np.array_equal(sim.fields()[0], ref.f()), pattern
+
+
+@pytest.mark.parametrize("corrections", [1, 2, 3])
+@pytest.mark.parametrize("pattern", ["pull", "aa"])
+def test_fp64_corrections_bit_exact(oracle_mod, pattern, corrections):
+    """The corrected boundary handling (bounce-back of every direction, of
+    inlet/outlet nodes too) against the oracle with the same corrections."""
+    O = oracle_mod
+    c = cases.vessel(4001)
+    geom = c.geometry()
+    sim = Simulation(geom, c.tau, c.boundary_specs(geom), precision="f64", pattern=pattern, corrections=corrections)
+    sim.step(21)
+    geo = O.geometry(c.triangles, c.spacing, c.grid, c.predicates)
+    ref = O.run_case(19, geo, c.tau, {0: (O.BC_VEL_NEGY, 1.0), 2: (O.BC_PRESS_POSY, c.outlet_rho)}, 21,
+                     profile=c.inlet_profile(geom), amp=c.amp_table(), corrections=corrections)
+    assert np.array_equal(sim.fields()[0], ref.f())
+
+
+def test_corrections_act_on_boundary_nodes_first():
+    """Parity and corrected runs differ, most at the boundary nodes (where the
+    bounce-back rules differ)."""
+    c = cases.pipe()
+    geom = c.geometry()
+    a = Simulation(geom, c.tau, c.boundary_specs(geom), precision="f64", pattern="pull")
+    b = Simulation(geom, c.tau, c.boundary_specs(geom), precision="f64", pattern="pull", corrections=3)
+    a.step(10)
+    b.step(10)
+    fa, fb = a.fields()[0], b.fields()[0]
+    d = np.abs(fa - fb).max(axis=1)
+    assert d.max() > 0
+    bnd = set(geom.list(_capi.LIST_BOUNDARY).tolist())
+    assert int(a.nodes()[np.argmax(d)]) in bnd

@@ -125,3 +125,122 @@ def test_oracle_equals_reference_d3q27_inlet(oracle_mod):
     sim = O.run_case(27, geo, c.tau, {0: (O.BC_VEL_POSX, 1.0)}, 8, profile=prof, amp=c.amp_table(),
                      inlet_dir=(1.0, 0.0, 0.0))
     assert np.array_equal(sim.f(), ref["f"])
+
+
+def test_face_zou_he_restates_every_reference_routine(oracle_mod):
+    """The generic face form of the oracle equals each reference Zou-He routine
+    on random populations (to rounding), except the f10 term of outlets 3-5
+    (Simulation.cpp:1124-1129), which changes f8 and f9 only."""
+    import numpy as np
+    O = oracle_mod
+    rng = np.random.default_rng(7)
+    w19 = np.array([2 / 36] * 6 + [1 / 36] * 12 + [12 / 36])
+    w27 = np.array([8 / 27] + [2 / 27] * 6 + [1 / 54] * 12 + [1 / 216] * 8)
+    cases = [(19, O.BC_VEL_NEGY, O.BC_FACE_VEL, O.FACE_NEGY, (0.01, -0.05, 0.02), 1.0),
+             (19, O.BC_PRESS_NEGY, O.BC_FACE_PRESS, O.FACE_NEGY, (0, 0, 0), 1.01),
+             (19, O.BC_PRESS_POSY, O.BC_FACE_PRESS, O.FACE_POSY, (0, 0, 0), 1.01),
+             (19, O.BC_PRESS_POSZ, O.BC_FACE_PRESS, O.FACE_POSZ, (0, 0, 0), 0.99),
+             (27, O.BC_VEL_POSX, O.BC_FACE_VEL, O.FACE_POSX, (0.04, 0.01, -0.02), 1.0)]
+    for Q, ref_kind, face_kind, face, v, rho in cases:
+        for _ in range(20):
+            f = (w19 if Q == 19 else w27) * (1 + 0.05 * rng.standard_normal(Q))
+            a = O.zou_he(Q, ref_kind, f, v, rho)
+            b = O.zou_he(Q, face_kind, f, v, rho, face)
+            assert np.abs(a - b).max() < 1e-15, (Q, ref_kind)
+    f = w19 * (1 + 0.05 * rng.standard_normal(19))
+    a = O.zou_he(19, O.BC_PRESS_POSX, f, rho=1.0)
+    b = O.zou_he(19, O.BC_FACE_PRESS, f, rho=1.0, face=O.FACE_POSX)
+    diff = np.flatnonzero(np.abs(a - b) > 1e-15)
+    assert list(diff) == [8, 9]
+    # the difference is the f10 - f16 term of Nxz, entering f8 with - and f9 with +
+    d = 0.5 * (f[10] - f[16])
+    assert abs((a[8] - b[8]) + d) < 1e-15 and abs((a[9] - b[9]) - d) < 1e-15
+
+
+def _transform(O, Q, role, dims, perm, flip):
+    """Role grid and direction map of an axis permutation + reflection:
+    new axis a holds old axis perm[a], reversed when flip[a]."""
+    r = role.reshape(dims)
+    r = np.transpose(r, perm)
+    for a in range(3):
+        if flip[a]:
+            r = np.flip(r, axis=a)
+    C = np.array(O_dirs(Q))
+    newc = C[:, list(perm)] * np.where(flip, -1, 1)
+    dmap = np.array([int(np.flatnonzero((C == newc[q]).all(1))[0]) for q in range(Q)])
+    return np.ascontiguousarray(r).reshape(-1), r.shape, dmap
+
+
+def O_dirs(Q):
+    from pv2013_gb300 import LatticeModel
+    L = LatticeModel(Q)
+    return [L.GetDirection(q) for q in range(Q)]
+
+
+def _run(O, Q, role, dims, bcs, faces, vel, tau, steps):
+    kinds = np.zeros(64, dtype=np.int32)
+    rho = np.ones(64)
+    for l, (k, r) in bcs.items():
+        kinds[l], rho[l] = k, r
+    sim = O.OracleSim(Q, dims, role, kinds, rho, tau)
+    for l, fc in faces.items():
+        sim.set_face(l, fc)
+    n = sim.list_size(0)
+    sim.set_velocity(0, np.tile(np.asarray(vel, dtype=np.float64), n))
+    sim.step(steps)
+    return sim.f()
+
+
+@pytest.mark.parametrize("Q", [19, 27])
+def test_face_kinds_are_covariant_under_axis_maps(oracle_mod, Q):
+    """The face kinds on a mirrored / axis-swapped lattice reproduce the
+    reference routines on the original one (to rounding): the derived
+    orientations are the reference's routines with the axes relabelled.
+    D3Q19 maps keep +x fixed, because the reference's bounce-back skips
+    direction 0 (Simulation.cpp:1361), which no other map preserves."""
+    O = oracle_mod
+    if Q == 19:
+        c = cases.pipe(radius=8.0, length=40.0, segments=32, ny=48, nxz=20)
+        geo = O.geometry(c.triangles, 1.0, c.grid, c.predicates)
+        base = {0: (O.BC_VEL_NEGY, 1.0), 2: (O.BC_PRESS_POSY, 1.0)}
+        vel = (0.0, -0.04, 0.0)
+        # inlet unknowns -y, outlet unknowns +y under each map
+        maps = [((0, 1, 2), (False, True, False)), ((0, 2, 1), (False, False, False)),
+                ((0, 2, 1), (False, False, True))]
+    else:
+        c = cases.pipe_x(radius=8.0, length=40.0, segments=32, nx=48, nyz=20)
+        geo = O.geometry(c.triangles, 1.0, c.grid, c.predicates)
+        base = {0: (O.BC_VEL_POSX, 1.0), 2: (O.BC_FACE_PRESS, 1.0)}
+        vel = (0.04, 0.0, 0.0)
+        maps = [((1, 0, 2), (False, False, False)), ((2, 1, 0), (True, False, False)),
+                ((0, 1, 2), (True, False, False))]
+    dims = tuple(geo["dims"])
+    steps = 30
+    base_faces = {2: O.FACE_NEGX} if Q == 27 else {}
+    f0 = _run(O, Q, geo["role"], dims, base, base_faces, vel, 0.8, steps)
+    C = np.array(O_dirs(Q))
+    grid0 = np.full(int(np.prod(dims)), -1)
+    grid0[geo["role"] >= 0] = np.arange(int((geo["role"] >= 0).sum()))
+    for perm, flip in maps:
+        role1, dims1, dmap = _transform(O, Q, geo["role"], dims, perm, flip)
+        # faces of the two lists in the new frame: image of the old unknown direction
+        def face_of(axis, sign):
+            v = np.zeros(3, dtype=int)
+            v[axis] = sign
+            w = v[list(perm)] * np.where(flip, -1, 1)
+            a = int(np.flatnonzero(w)[0])
+            return 2 * a + (1 if w[a] < 0 else 0)
+        if Q == 19:
+            faces = {0: face_of(1, -1), 2: face_of(1, 1)}
+        else:
+            faces = {0: face_of(0, 1), 2: face_of(0, -1)}
+        bcs = {0: (O.BC_FACE_VEL, 1.0), 2: (O.BC_FACE_PRESS, 1.0)}
+        vel1 = np.asarray(vel)[list(perm)] * np.where(flip, -1, 1)
+        f1 = _run(O, Q, role1, dims1, bcs, faces, vel1, 0.8, steps)
+        # node correspondence through the grid map
+        g1 = np.transpose(grid0.reshape(dims), perm)
+        for a in range(3):
+            if flip[a]:
+                g1 = np.flip(g1, axis=a)
+        ids0 = g1.reshape(-1)[role1 >= 0]          # old node id of every new node, new order
+        assert np.abs(f1[:, dmap] - f0[ids0]).max() < 1e-14, (perm, flip)
