@@ -277,6 +277,24 @@ def gpu_arm(args, rank, world):
     h2d = case.triangles.nbytes + 8 * len(case.inlet_profile(geom)) + 8 * len(case.amp_table())
     d2h = rho_h.nbytes + u_h.nbytes
 
+    # --- batched: the 64-vessel ensemble in one launch per step --------------
+    batched = None
+    if not args.no_batch:
+        ens = cases.ensemble(64)
+        egeo = [c.geometry() for c in ens]
+        enf = sum(g.info.n_fluid for g in egeo)
+        esim = Simulation(egeo, [c.tau for c in ens], [c.boundary_specs(g) for c, g in zip(ens, egeo)],
+                          precision="f16s", pattern=args.pattern)
+        esim.autotune(launches=10)
+        esec = time_steps(esim, args.batch_steps, args.warmup, torch)
+        einfo = esim.info()
+        batched = {"workload": "ensemble of 64 tortuous vessels (seeds 4000-4063), per-instance tau, inlet amplitude "
+                               "and period, FP16-shifted AA, one launch per step",
+                   "fluid_nodes": enf, "steps": args.batch_steps, "mlups": enf * args.batch_steps / esec / 1e6 * world,
+                   "ms_per_step": esec / args.batch_steps * 1e3,
+                   "kernel": {"nodes_per_lane": einfo.nodes_per_lane, "warps_per_block": einfo.warps_per_block}}
+        del esim, egeo
+
     # --- roofline of the step kernel ------------------------------------------
     launch_s = sec16 / args.steps
     achieved = bpu16 * nf / launch_s / 1e9
@@ -316,6 +334,7 @@ def gpu_arm(args, rank, world):
         "fp32_pull_paired_mlups": mlups32p,
         "error_vs_fp64": {"steps": err_steps, "u_rel_l2": u_l2, "u_rel_max": u_max, "rho_max_abs": rho_drift,
                           "mass_change_per_1000_steps": mass_loss_per_1000},
+        "batched": batched,
         "roofline": roof, "cpu_baseline": cpu,
         "e2e": {"value": e2e_mlups, "unit": "MLUPS", "h2d_bytes_per_step": h2d / e2e_steps,
                 "d2h_bytes_per_step": d2h / e2e_steps,
@@ -338,6 +357,8 @@ def main():
     ap.add_argument("--nodes-per-lane", type=int, default=0, help="0 = engine default (paired), 1 or 2")
     ap.add_argument("--err-steps", type=int, default=500)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the 64-vessel ensemble line")
+    ap.add_argument("--batch-steps", type=int, default=1000)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -9,8 +9,9 @@ BF16-shifted storage runs (FP32 collision math) advance the same case; the
 study reports, per storage, the velocity error relative to FP64 (L2 and max,
 relative to the FP64 field's L2 norm and maximum), the largest density
 difference, the relative mass change per 1000 steps, and MLUPS.  A run whose
-monitors report non-finite values or a mass drift above 1 % is reported as
-diverged, with the step at which it was detected.
+monitors report non-finite values or a mass change above 50 % is reported
+as diverged, with the step at which it was detected (checked every 500
+steps).
 
 ensemble: n tortuous vessels (cases.vessel, per-instance tau, inlet
 amplitude and period) advance together in one launch per step over a packed
@@ -48,7 +49,8 @@ def face_specs(case, geom, Q):
 
 
 def _timed_run(sim, steps, chunk=500):
-    """Advances in chunks with the divergence monitor; returns (seconds, diverged_at or None)."""
+    """Advances in chunks with the divergence monitor; returns (seconds,
+    None) or, when the monitor trips, (seconds, the step count reached)."""
     import torch
     torch.cuda.synchronize()
     t0 = time.time()
@@ -74,18 +76,18 @@ def precision_study(case, Q, taus, steps, precisions=("f32", "f16s", "bf16s")):
     for tau in taus:
         specs = face_specs(case, geom, Q)
         ref = Simulation(geom, tau, specs, Q=Q, precision="f64", pattern="pull")
-        ref.set_divergence_tolerance(1e-2)
+        ref.set_divergence_tolerance(0.5)
         sec, div = _timed_run(ref, steps)
-        row = {"tau": tau, "f64": {"mlups": nf * steps / sec / 1e6, "diverged_at": div}}
+        row = {"tau": tau, "f64": {"mlups": nf * (div or steps) / sec / 1e6, "diverged_at": div}}
         if div is None:
             _, r64, u64 = ref.fields(f=False)
         del ref
         for prec in precisions:
             sim = Simulation(geom, tau, face_specs(case, geom, Q), Q=Q, precision=prec, pattern="aa")
-            sim.set_divergence_tolerance(1e-2)
+            sim.set_divergence_tolerance(0.5)
             m0 = sim.monitors()["mass"]
             sec, d = _timed_run(sim, steps)
-            r = {"mlups": nf * steps / sec / 1e6, "diverged_at": d}
+            r = {"mlups": nf * (d or steps) / sec / 1e6, "diverged_at": d}
             if d is None and div is None:
                 _, rr, uu = sim.fields(f=False)
                 m1 = sim.monitors()["mass"]
