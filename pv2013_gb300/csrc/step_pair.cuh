@@ -257,12 +257,12 @@ __device__ __forceinline__ void collide2(const typename PairWord<S>::W* raw, flo
 }
 
 // register budget per thread: D3Q19 with 16-bit storage holds one 32-bit
-// word per population: 64 registers (4 blocks of 256) for the node-local and
-// pull patterns, 80 (3 blocks) for the AA odd pattern, which keeps its eight
-// column bases across the collision for the scatter; FP32 storage (two
-// registers per word) and D3Q27 get 128 (2 blocks)
+// word per population: 64 registers (4 blocks of 256; measured faster than 80
+// registers for the AA odd pattern, whose occupancy matters more than its few
+// spilled values); FP32 storage (two registers per word) and D3Q27 get 128
+// (2 blocks)
 template <int Q, int S, int MODE> struct PairMinBlocks {
-    static constexpr int value = (Q == 19 && S != ST_F32) ? (MODE == MODE_AA_ODD ? 3 : 4) : 2;
+    static constexpr int value = (Q == 19 && S != ST_F32) ? 4 : 2;
 };
 
 template <int Q, int S, int MODE, int RA>
@@ -315,9 +315,16 @@ __global__ void __launch_bounds__(256, PairMinBlocks<Q, S, MODE>::value) k_step2
     };
 
     W raw[Q];
+    __shared__ int32_t ksm[8][2][8];     // column bases of each warp's two chunks
     if (act) {
         int32_t K[8];
         if constexpr (MODE != MODE_AA_EVEN) load_K(K, false);
+        if constexpr (MODE == MODE_AA_ODD) {
+            if (t == 0) {
+#pragma unroll
+                for (int c = 0; c < 8; ++c) ksm[threadIdx.x >> 5][lane >> 4][c] = K[c];
+            }
+        }
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
             if constexpr (MODE == MODE_AA_EVEN) {
@@ -333,6 +340,9 @@ __global__ void __launch_bounds__(256, PairMinBlocks<Q, S, MODE>::value) k_step2
         }
     }
 
+    // the odd pattern's column bases go through shared memory (lane 0 of
+    // each chunk wrote them): fewer registers held across the collision
+    if constexpr (MODE == MODE_AA_ODD) __syncwarp();
     // missing populations (boundary nodes): bounce-back or the initial value
     if (__any_sync(0xffffffffu, (m_lo | m_hi) != 0u)) {
         uint32_t wm = 0u;
@@ -392,11 +402,10 @@ __global__ void __launch_bounds__(256, PairMinBlocks<Q, S, MODE>::value) k_step2
         uint32_t vm;
         asm volatile("ld.global.nc.u32 %0, [%1];" : "=r"(vm) : "l"(&cw[3].w));
         vm = (vm >> (2 * t)) & 3u;
-        int32_t K[8];
-        load_K(K, true);
+        const volatile int32_t* ks = ksm[threadIdx.x >> 5][lane >> 4];
         collide2<Q, S>(raw, om, [&](int q, F2 v) {
             const int da = X::a(q), db = X::b(q), o = X::r(q);
-            const uint32_t s = (uint32_t)((da == 0 && db == 0 ? n0 - 1 : K[col8(da, db)]) + 1 + 2 * t);
+            const uint32_t s = (uint32_t)((da == 0 && db == 0 ? n0 - 1 : ks[col8(da, db)]) + 1 + 2 * t);
             const bool bl = (m_lo >> L::opp(q)) & 1u, bh = (m_hi >> L::opp(q)) & 1u;
             const uint32_t pq = (uint32_t)q * st, po = (uint32_t)L::opp(q) * st;
             if (o == 0 && vm == 3u && !bl && !bh) {
