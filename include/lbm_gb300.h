@@ -319,6 +319,56 @@ lbm_status lbm_sim_set_divergence_tolerance(lbm_sim* s, double rel_tol);
 void lbm_sim_destroy(lbm_sim* s);
 
 /* ------------------------------------------------------------------------ */
+/* Output: wall shear stress and VTK snapshots (OutputFile.cpp:16-137).      */
+
+/* Wall shear stress of the current state at every wall node, in the wall
+ * list's order (lbm_geometry_list(LBM_LIST_WALL), instances concatenated):
+ * |mu g| with g the mean of u(x + c_q) - u(x) over the neighbours that are
+ * fluid points (q = 0..Q-1, the rest direction included) and
+ * mu = (2 tau - 1)/6 (Simulation.cpp:1374-1421).  u is the velocity of the
+ * current populations -- the value the reference's next Collision stores, so
+ * after n steps this is the reference's wall shear stress of iteration n.
+ * wss may be NULL to query *n. */
+lbm_status lbm_sim_wall_shear_stress(lbm_sim* s, double* wss, size_t cap, size_t* n, void* stream);
+
+/* Point-data .vtu writer: n points (xyz, 3 floats each), VTK_VERTEX cells,
+ * Float64 arrays; raw appended binary. */
+typedef struct lbm_vtu_array {
+    const char* name;
+    int32_t components;
+    int32_t reserved;
+    const double* data;        /* n * components values */
+} lbm_vtu_array;
+lbm_status lbm_vtu_write(const char* path, size_t n, const float* xyz, size_t narrays, const lbm_vtu_array* arrays);
+
+/* Asynchronous snapshots.  lbm_snapshot_capture enqueues, on the caller's
+ * stream, one snapshot launch of the current state (rho, u and, with
+ * LBM_SNAP_WSS, the wall shear stress) into device buffers of the snapshot,
+ * then copies them to the snapshot's pinned host buffers on a stream of its
+ * own and returns: the simulation can keep stepping on its stream while the
+ * copy runs.  lbm_snapshot_wait blocks until the host buffers hold the
+ * capture; the write functions wait, then write the reference's files:
+ *   fields: points at the nodes' lattice indices, x fastest (the loop order of
+ *           WriteVTK_LocalData), arrays Velocity, Pressure (c_s^2 rho),
+ *           VelocityMagnitude, Density -- all of the captured state (the
+ *           reference's Pressure is summed from the populations one step
+ *           later than its other arrays, OutputFile.cpp:64);
+ *   wss:    the wall nodes in wall-list order, array WallShearStress.
+ * One capture in flight per snapshot; a batch writes one instance per file. */
+#define LBM_SNAP_FIELDS 1
+#define LBM_SNAP_WSS 2
+typedef struct lbm_snapshot lbm_snapshot;
+lbm_status lbm_snapshot_create(lbm_sim* s, uint32_t what, lbm_snapshot** out);
+lbm_status lbm_snapshot_capture(lbm_snapshot* snap, void* stream);
+lbm_status lbm_snapshot_wait(lbm_snapshot* snap);
+/* Host views of the last capture (valid until the next capture or destroy). */
+lbm_status lbm_snapshot_data(lbm_snapshot* snap, const double** rho, const double** u, const double** wss,
+                             size_t* n_nodes, size_t* n_wall, int64_t* step);
+lbm_status lbm_snapshot_write_fields_vtu(lbm_snapshot* snap, const char* path, int32_t instance);
+lbm_status lbm_snapshot_write_wss_vtu(lbm_snapshot* snap, const char* path, int32_t instance);
+void lbm_snapshot_destroy(lbm_snapshot* snap);
+
+/* ------------------------------------------------------------------------ */
 /* Synthetic geometry generators (seeded, deterministic).                    */
 
 /* Triangulated cylinder: radius r, length len, `segments` facets around,

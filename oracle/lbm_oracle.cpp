@@ -394,6 +394,7 @@ void orc_sim_destroy(void* h) { delete (OrcSim*)h; }
 int64_t orc_sim_nodes(void* h) { return ((OrcSim*)h)->N; }
 int64_t orc_sim_list_size(void* h, int l) { return (int64_t)((OrcSim*)h)->lists[l].size(); }
 int64_t orc_sim_zero_hits(void* h) { return ((OrcSim*)h)->zero_hits; }
+int64_t orc_sim_wall_count(void* h) { return (int64_t)((OrcSim*)h)->wall.size(); }
 
 void orc_sim_set_face(void* h, int l, int face) { ((OrcSim*)h)->list_face[l] = face; }
 
@@ -642,6 +643,30 @@ void orc_sim_step(void* h, int nsteps) {
                 bc_press(&s->f[(size_t)s->lists[l][m] * Q], k, s->list_rho[l]);
         }
         s->steps++;
+    }
+}
+
+// Wall shear stress of every wall node, wall-list order, from the velocities
+// of the last collision (ComputeVelocityGradientAtWall and
+// ComputeWallShearStress, Simulation.cpp:1374-1421).
+void orc_sim_wss(void* h, double* out) {
+    OrcSim* s = (OrcSim*)h;
+    const int Q = s->Q;
+    const double mu = 1.0 / 6.0 * (2.0 * s->tau - 1.0);
+    for (size_t m = 0; m < s->wall.size(); ++m) {
+        const int32_t n = s->wall[m];
+        double g[3] = {0.0, 0.0, 0.0};
+        int cnt = 0;
+        for (int d = 0; d < Q; ++d) {
+            const int32_t nb = s->nbr[(size_t)n * Q + d];
+            if (nb < 0) continue;
+            for (int k = 0; k < 3; ++k) g[k] += (s->u[3 * (size_t)nb + k] - s->u[3 * (size_t)n + k]);
+            ++cnt;
+        }
+        if (cnt > 0)
+            for (int k = 0; k < 3; ++k) g[k] /= cnt;
+        const double s0 = mu * g[0], s1 = mu * g[1], s2 = mu * g[2];
+        out[m] = std::sqrt(s0 * s0 + s1 * s1 + s2 * s2);
     }
 }
 

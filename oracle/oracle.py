@@ -72,6 +72,9 @@ def lib():
         L.orc_sim_set_velocity.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
         L.orc_sim_set_face.argtypes = [C.c_void_p, C.c_int, C.c_int]
         L.orc_sim_set_corrections.argtypes = [C.c_void_p, C.c_int]
+        L.orc_sim_wss.argtypes = [C.c_void_p, C.c_void_p]
+        L.orc_sim_wall_count.restype = C.c_int64
+        L.orc_sim_wall_count.argtypes = [C.c_void_p]
         L.orc_zou_he.argtypes = [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p, C.c_double]
         L.orc_sim_step.argtypes = [C.c_void_p, C.c_int]
         L.orc_sim_get.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
@@ -243,6 +246,12 @@ class OracleSim:
 
     def zero_hits(self):
         return self.L.orc_sim_zero_hits(self.h)
+
+    def wss(self):
+        """Wall shear stress per wall node (wall-list order) from the last collision's velocities."""
+        out = np.empty(self.L.orc_sim_wall_count(self.h))
+        self.L.orc_sim_wss(self.h, _p(out))
+        return out
 
     def f(self):
         out = np.empty((self.n, self.Q))

@@ -4,8 +4,8 @@ Zou-He and bounce-back boundaries, as sm_103a CUDA kernels behind the C ABI
 of include/lbm_gb300.h (liblbm_gb300.so, built in-tree)."""
 from . import _capi
 from ._capi import LbmError, load
-from .engine import (BoundarySpec, Geometry, LatticeModel, PlanePredicate, Reader, Simulation,
-                     pv2013_predicates, synth_capsules, synth_cylinder)
+from .engine import (BoundarySpec, Geometry, LatticeModel, PlanePredicate, Reader, Simulation, Snapshot,
+                     pv2013_predicates, synth_capsules, synth_cylinder, write_vtu)
 
 __all__ = ["BoundarySpec", "Geometry", "LatticeModel", "LbmError", "PlanePredicate", "Reader", "Simulation",
-           "load", "pv2013_predicates", "synth_capsules", "synth_cylinder", "_capi"]
+           "Snapshot", "load", "pv2013_predicates", "synth_capsules", "synth_cylinder", "write_vtu", "_capi"]

@@ -29,6 +29,7 @@ FACE_POSX, FACE_NEGX, FACE_POSY, FACE_NEGY, FACE_POSZ, FACE_NEGZ = range(6)
 LIST_BOUNDARY, LIST_WALL = -1, -2
 STEP_GRAPH, STEP_MONITOR = 1, 2
 FIX_BB_ALL_DIRS, FIX_LIST_NODES = 1, 2
+SNAP_FIELDS, SNAP_WSS = 1, 2
 
 
 class LbmError(RuntimeError):
@@ -78,6 +79,11 @@ class TuneEntry(C.Structure):
                 ("chosen", C.c_int32), ("ms_per_launch", C.c_double)]
 
 
+class VtuArray(C.Structure):
+    _fields_ = [("name", C.c_char_p), ("components", C.c_int32), ("reserved", C.c_int32),
+                ("data", C.POINTER(C.c_double))]
+
+
 class SimInfo(C.Structure):
     _fields_ = [("n_nodes", C.c_int64), ("n_instances", C.c_int64), ("steps_done", C.c_int64),
                 ("n_chunks", C.c_int64), ("Q", C.c_int32), ("precision", C.c_int32), ("pattern", C.c_int32),
@@ -115,6 +121,16 @@ PROTOTYPES = {
     "lbm_sim_fields": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
     "lbm_sim_fields_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
     "lbm_sim_autotune": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]),
+    "lbm_sim_wall_shear_stress": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p]),
+    "lbm_vtu_write": (C.c_int, [C.c_char_p, C.c_size_t, C.c_void_p, C.c_size_t, C.c_void_p]),
+    "lbm_snapshot_create": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p]),
+    "lbm_snapshot_capture": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "lbm_snapshot_wait": (C.c_int, [C.c_void_p]),
+    "lbm_snapshot_data": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                    C.c_void_p]),
+    "lbm_snapshot_write_fields_vtu": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int32]),
+    "lbm_snapshot_write_wss_vtu": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int32]),
+    "lbm_snapshot_destroy": (None, [C.c_void_p]),
     "lbm_sim_nodes": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "lbm_sim_instance_offsets": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "lbm_sim_monitors": (C.c_int, [C.c_void_p, _P(Monitors), C.c_void_p]),

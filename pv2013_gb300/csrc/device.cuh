@@ -122,6 +122,7 @@ struct InstParam {
     double omega;      // 1/tau
     float omega_f;
     float pad;
+    double tau;
 };
 
 // Storage formats.  Shifted formats hold (f - w) scaled; FP64/FP32 hold f.

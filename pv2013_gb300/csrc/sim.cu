@@ -19,6 +19,7 @@
 // reference's Inlet, Outlet1..6 order); boundary points in no list are wall
 // nodes; other fluid points are interior nodes.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -505,6 +506,10 @@ struct lbm_sim {
     int64_t part_blocks = 0;
     double mass0 = 0.0;
     double div_tol = 1e-2;
+    // wall nodes: output positions in wall-list order (built on first use)
+    int64_t* wall_pos = nullptr;
+    int64_t nwall = -1;
+    std::vector<std::array<int, 3>> dims;   // grid of each instance
 };
 
 namespace {
@@ -864,6 +869,11 @@ lbm_status sim_create(const lbm_geometry* const* g, const lbm_sim_params* p, siz
         if (geometry_device(g[i]) != S->dev) return fail(LBM_ERR_ARG, "geometry %zu lives on another device", i);
     }
     S->n_inst = (int64_t)n;
+    for (size_t i = 0; i < n; ++i) {
+        int d[3];
+        geometry_dims(g[i], d);
+        S->dims.push_back({d[0], d[1], d[2]});
+    }
     if (p0.run_axis != 0) {
         S->ra = p0.run_axis;
     } else {
@@ -943,6 +953,7 @@ lbm_status sim_create(const lbm_geometry* const* g, const lbm_sim_params* p, siz
         insts[i].omega = 1.0 / p[i].tau;
         insts[i].omega_f = (float)insts[i].omega;
         insts[i].pad = 0.f;
+        insts[i].tau = p[i].tau;
         for (int l = 0; l < 64; ++l) {
             ListParam& L = lists[64 * i + l];
             std::memset(&L, 0, sizeof L);
@@ -1015,6 +1026,81 @@ lbm_status sim_create(const lbm_geometry* const* g, const lbm_sim_params* p, siz
     LBM_TRY(sim_monitors(S.get(), &m, st));
     S->mass0 = m.mass;
     *out = S.release();
+    return LBM_OK;
+}
+
+__global__ void k_gather_f64(const double* __restrict__ src, const int64_t* __restrict__ idx, int64_t n,
+                             double* __restrict__ dst) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        dst[i] = src[idx[i]];
+}
+
+// Output positions of the wall nodes in wall-list order (the x-major order of
+// the outputs), found once from the chunk masks.
+lbm_status sim_wall_positions(lbm_sim* S, const double* d_u, double* d_wss_pos, cudaStream_t st) {
+    if (S->nwall >= 0) return LBM_OK;
+    DBuf<uint8_t> flag;
+    LBM_TRY(flag.alloc(S->NF, "wall flags"));
+    LBM_CUDA(cudaMemsetAsync(flag.p, 0, S->NF, st));
+    LBM_TRY(launch_wss(S->Q, S->ra, S->chunks, S->nchunks, S->mmask, S->out_pos, S->insts, d_u, d_wss_pos, flag.p, st));
+    int64_t* idx = nullptr;
+    int64_t cnt = 0;
+    LBM_TRY(scan::compact(flag.p, S->NF, &idx, &cnt, st));
+    S->wall_pos = idx;
+    S->nwall = cnt;
+    return LBM_OK;
+}
+
+// rho, u of the current state into d_rho / d_u (either may be null), and the
+// wall shear stress in wall-list order into d_wss (needs d_u and an NF-sized
+// scratch d_wss_pos).
+lbm_status sim_outputs(lbm_sim* S, double* d_rho, double* d_u, double* d_wss_pos, double* d_wss, cudaStream_t st) {
+    LBM_TRY(sim_dry(S, nullptr, d_rho, d_u, false, st));
+    if (d_wss) {
+        LBM_TRY(sim_wall_positions(S, d_u, d_wss_pos, st));
+        LBM_TRY(launch_wss(S->Q, S->ra, S->chunks, S->nchunks, S->mmask, S->out_pos, S->insts, d_u, d_wss_pos,
+                           nullptr, st));
+        if (S->nwall > 0)
+            k_gather_f64<<<blocks_for(S->nwall, 256), 256, 0, st>>>(d_wss_pos, S->wall_pos, S->nwall, d_wss);
+        LBM_CUDA(cudaGetLastError());
+    }
+    return LBM_OK;
+}
+
+}  // namespace
+
+struct lbm_snapshot {
+    lbm_sim* S = nullptr;
+    uint32_t what = 0;
+    double *d_rho = nullptr, *d_u = nullptr, *d_wss_pos = nullptr, *d_wss = nullptr;
+    double *h_rho = nullptr, *h_u = nullptr, *h_wss = nullptr;
+    int64_t n = 0, nwall = 0, step = -1;
+    cudaStream_t copy = nullptr;
+    cudaEvent_t computed = nullptr, ready = nullptr;
+    bool pending = false;
+    std::vector<int64_t> grid, inst_off;        // output grid indices, instance offsets
+    std::vector<int64_t> wall_inst_off;         // wall nodes per instance (offsets)
+    std::vector<int64_t> wall_grid_pos_;        // output position of each wall node
+};
+
+namespace {
+
+void snapshot_free(lbm_snapshot* P) {
+    if (P->pending && P->ready) cudaEventSynchronize(P->ready);
+    for (double* d : {P->d_rho, P->d_u, P->d_wss_pos, P->d_wss}) if (d) cudaFree(d);
+    for (double* h : {P->h_rho, P->h_u, P->h_wss}) if (h) cudaFreeHost(h);
+    if (P->computed) cudaEventDestroy(P->computed);
+    if (P->ready) cudaEventDestroy(P->ready);
+    if (P->copy) cudaStreamDestroy(P->copy);
+    delete P;
+}
+
+lbm_status snapshot_wait(lbm_snapshot* P) {
+    if (P->pending) {
+        LBM_CUDA(cudaEventSynchronize(P->ready));
+        P->pending = false;
+    }
+    if (P->step < 0) return fail(LBM_ERR_STATE, "snapshot: nothing captured yet");
     return LBM_OK;
 }
 
@@ -1320,12 +1406,194 @@ lbm_status lbm_sim_set_divergence_tolerance(lbm_sim* S, double rel_tol) {
     return LBM_OK;
 }
 
+lbm_status lbm_sim_wall_shear_stress(lbm_sim* S, double* wss, size_t cap, size_t* n, void* stream) {
+    if (!S) return fail(LBM_ERR_ARG, "lbm_sim_wall_shear_stress: null handle");
+    clear_error();
+    cudaStream_t st = (cudaStream_t)stream;
+    DBuf<double> du, dpos, dw;
+    LBM_TRY(du.alloc((size_t)S->NF * 3, "velocity"));
+    LBM_TRY(dpos.alloc(S->NF, "wall shear stress"));
+    LBM_TRY(check_timeout(S, st));
+    LBM_TRY(sim_dry(S, nullptr, nullptr, du.p, false, st));
+    LBM_TRY(sim_wall_positions(S, du.p, dpos.p, st));
+    if (n) *n = (size_t)S->nwall;
+    if (!wss) {
+        LBM_CUDA(cudaStreamSynchronize(st));
+        return LBM_OK;
+    }
+    if (cap < (size_t)S->nwall) return fail(LBM_ERR_ARG, "lbm_sim_wall_shear_stress: capacity %zu < %lld wall nodes", cap,
+                                            (long long)S->nwall);
+    LBM_TRY(dw.alloc(S->nwall, "wall shear stress"));
+    LBM_TRY(sim_outputs(S, nullptr, du.p, dpos.p, dw.p, st));
+    if (S->nwall) LBM_CUDA(cudaMemcpyAsync(wss, dw.p, sizeof(double) * S->nwall, cudaMemcpyDeviceToHost, st));
+    LBM_CUDA(cudaStreamSynchronize(st));
+    return LBM_OK;
+}
+
+lbm_status lbm_snapshot_create(lbm_sim* S, uint32_t what, lbm_snapshot** out) {
+    if (!S || !out || !what || (what & ~(uint32_t)(LBM_SNAP_FIELDS | LBM_SNAP_WSS)))
+        return fail(LBM_ERR_ARG, "lbm_snapshot_create: bad argument");
+    clear_error();
+    *out = nullptr;
+    std::unique_ptr<lbm_snapshot, void (*)(lbm_snapshot*)> P(new lbm_snapshot(), snapshot_free);
+    P->S = S;
+    P->what = what;
+    P->n = S->NF;
+    const size_t n = (size_t)S->NF;
+    auto dmal = [&](double** p, size_t cnt, const char* what_) -> lbm_status {
+        if (cudaMalloc(p, sizeof(double) * (cnt ? cnt : 1)) != cudaSuccess)
+            return fail(LBM_ERR_NOMEM, "snapshot: cudaMalloc for %s failed", what_);
+        return LBM_OK;
+    };
+    auto hmal = [&](double** p, size_t cnt, const char* what_) -> lbm_status {
+        if (cudaHostAlloc(p, sizeof(double) * (cnt ? cnt : 1), cudaHostAllocDefault) != cudaSuccess)
+            return fail(LBM_ERR_NOMEM, "snapshot: pinned host allocation for %s failed", what_);
+        return LBM_OK;
+    };
+    LBM_TRY(dmal(&P->d_u, 3 * n, "velocity"));
+    if (what & LBM_SNAP_FIELDS) {
+        LBM_TRY(dmal(&P->d_rho, n, "density"));
+        LBM_TRY(hmal(&P->h_rho, n, "density"));
+        LBM_TRY(hmal(&P->h_u, 3 * n, "velocity"));
+    }
+    if (what & LBM_SNAP_WSS) {
+        LBM_TRY(dmal(&P->d_wss_pos, n, "wall shear stress"));
+        LBM_TRY(sim_outputs(S, nullptr, P->d_u, nullptr, nullptr, nullptr));   // velocities for the wall search
+        LBM_TRY(sim_wall_positions(S, P->d_u, P->d_wss_pos, nullptr));
+        P->nwall = S->nwall;
+        LBM_TRY(dmal(&P->d_wss, P->nwall, "wall shear stress"));
+        LBM_TRY(hmal(&P->h_wss, P->nwall, "wall shear stress"));
+    }
+    LBM_CUDA(cudaStreamCreateWithFlags(&P->copy, cudaStreamNonBlocking));
+    LBM_CUDA(cudaEventCreateWithFlags(&P->computed, cudaEventDisableTiming));
+    LBM_CUDA(cudaEventCreateWithFlags(&P->ready, cudaEventDisableTiming));
+    // node and wall coordinates per instance (host copies)
+    P->grid.resize(n);
+    LBM_CUDA(cudaMemcpy(P->grid.data(), S->node_grid, sizeof(int64_t) * n, cudaMemcpyDeviceToHost));
+    P->inst_off = S->inst_off;
+    if (what & LBM_SNAP_WSS) {
+        std::vector<int64_t> wp((size_t)P->nwall);
+        if (P->nwall) LBM_CUDA(cudaMemcpy(wp.data(), S->wall_pos, sizeof(int64_t) * P->nwall, cudaMemcpyDeviceToHost));
+        P->wall_inst_off.assign(1, 0);
+        size_t w = 0;
+        for (size_t i = 0; i + 1 < P->inst_off.size(); ++i) {
+            while (w < wp.size() && wp[w] < P->inst_off[i + 1]) ++w;
+            P->wall_inst_off.push_back((int64_t)w);
+        }
+        P->wall_grid_pos_ = std::move(wp);
+    }
+    *out = P.release();
+    return LBM_OK;
+}
+
+lbm_status lbm_snapshot_capture(lbm_snapshot* P, void* stream) {
+    if (!P) return fail(LBM_ERR_ARG, "lbm_snapshot_capture: null handle");
+    clear_error();
+    if (P->pending) LBM_CUDA(cudaEventSynchronize(P->ready));   // one capture in flight
+    cudaStream_t st = (cudaStream_t)stream;
+    lbm_sim* S = P->S;
+    LBM_TRY(check_timeout(S, st));
+    LBM_TRY(sim_outputs(S, P->d_rho, P->d_u, P->d_wss_pos, P->d_wss, st));
+    LBM_CUDA(cudaEventRecord(P->computed, st));
+    LBM_CUDA(cudaStreamWaitEvent(P->copy, P->computed, 0));
+    const size_t n = (size_t)P->n;
+    if (P->what & LBM_SNAP_FIELDS) {
+        LBM_CUDA(cudaMemcpyAsync(P->h_rho, P->d_rho, sizeof(double) * n, cudaMemcpyDeviceToHost, P->copy));
+        LBM_CUDA(cudaMemcpyAsync(P->h_u, P->d_u, sizeof(double) * 3 * n, cudaMemcpyDeviceToHost, P->copy));
+    }
+    if ((P->what & LBM_SNAP_WSS) && P->nwall)
+        LBM_CUDA(cudaMemcpyAsync(P->h_wss, P->d_wss, sizeof(double) * P->nwall, cudaMemcpyDeviceToHost, P->copy));
+    LBM_CUDA(cudaEventRecord(P->ready, P->copy));
+    P->pending = true;
+    P->step = S->steps_done;
+    return LBM_OK;
+}
+
+lbm_status lbm_snapshot_wait(lbm_snapshot* P) {
+    if (!P) return fail(LBM_ERR_ARG, "lbm_snapshot_wait: null handle");
+    clear_error();
+    return snapshot_wait(P);
+}
+
+lbm_status lbm_snapshot_data(lbm_snapshot* P, const double** rho, const double** u, const double** wss, size_t* n_nodes,
+                             size_t* n_wall, int64_t* step) {
+    if (!P) return fail(LBM_ERR_ARG, "lbm_snapshot_data: null handle");
+    clear_error();
+    LBM_TRY(snapshot_wait(P));
+    if (rho) *rho = P->h_rho;
+    if (u) *u = P->h_u;
+    if (wss) *wss = P->h_wss;
+    if (n_nodes) *n_nodes = (size_t)P->n;
+    if (n_wall) *n_wall = (size_t)P->nwall;
+    if (step) *step = P->step;
+    return LBM_OK;
+}
+
+lbm_status lbm_snapshot_write_fields_vtu(lbm_snapshot* P, const char* path, int32_t instance) {
+    if (!P || !path) return fail(LBM_ERR_ARG, "lbm_snapshot_write_fields_vtu: null argument");
+    if (!(P->what & LBM_SNAP_FIELDS)) return fail(LBM_ERR_STATE, "snapshot was created without LBM_SNAP_FIELDS");
+    if (instance < 0 || instance >= (int32_t)P->S->n_inst) return fail(LBM_ERR_ARG, "instance %d out of range", instance);
+    clear_error();
+    LBM_TRY(snapshot_wait(P));
+    const std::array<int, 3>& d = P->S->dims[instance];
+    const int64_t b = P->inst_off[instance], e = P->inst_off[instance + 1], m = e - b;
+    // the reference's loop order: z outermost, x fastest (OutputFile.cpp:43-45)
+    std::vector<int64_t> order((size_t)m);
+    for (int64_t i = 0; i < m; ++i) order[(size_t)i] = b + i;
+    auto key = [&](int64_t o) {
+        const int64_t g = P->grid[(size_t)o];
+        const int64_t i = g / ((int64_t)d[1] * d[2]), j = (g / d[2]) % d[1], k = g % d[2];
+        return (k * d[1] + j) * (int64_t)d[0] + i;
+    };
+    std::sort(order.begin(), order.end(), [&](int64_t x, int64_t y) { return key(x) < key(y); });
+    std::vector<float> xyz(3 * (size_t)m);
+    std::vector<double> vel(3 * (size_t)m), pres((size_t)m), mag((size_t)m), rho((size_t)m);
+    for (int64_t t = 0; t < m; ++t) {
+        const int64_t o = order[(size_t)t], g = P->grid[(size_t)o];
+        xyz[3 * t] = (float)(g / ((int64_t)d[1] * d[2]));
+        xyz[3 * t + 1] = (float)((g / d[2]) % d[1]);
+        xyz[3 * t + 2] = (float)(g % d[2]);
+        const double ux = P->h_u[3 * o], uy = P->h_u[3 * o + 1], uz = P->h_u[3 * o + 2];
+        vel[3 * t] = ux; vel[3 * t + 1] = uy; vel[3 * t + 2] = uz;
+        rho[t] = P->h_rho[o];
+        pres[t] = (1.0 / 3.0) * P->h_rho[o];     // Node::Pressure: c_s^2 rho (Node.cpp:112-118)
+        mag[t] = std::sqrt(ux * ux + uy * uy + uz * uz);
+    }
+    const lbm_vtu_array arr[4] = {{"Velocity", 3, 0, vel.data()}, {"Pressure", 1, 0, pres.data()},
+                                  {"VelocityMagnitude", 1, 0, mag.data()}, {"Density", 1, 0, rho.data()}};
+    return lbm_vtu_write(path, (size_t)m, xyz.data(), 4, arr);
+}
+
+lbm_status lbm_snapshot_write_wss_vtu(lbm_snapshot* P, const char* path, int32_t instance) {
+    if (!P || !path) return fail(LBM_ERR_ARG, "lbm_snapshot_write_wss_vtu: null argument");
+    if (!(P->what & LBM_SNAP_WSS)) return fail(LBM_ERR_STATE, "snapshot was created without LBM_SNAP_WSS");
+    if (instance < 0 || instance >= (int32_t)P->S->n_inst) return fail(LBM_ERR_ARG, "instance %d out of range", instance);
+    clear_error();
+    LBM_TRY(snapshot_wait(P));
+    const std::array<int, 3>& d = P->S->dims[instance];
+    const int64_t b = P->wall_inst_off[instance], e = P->wall_inst_off[instance + 1], m = e - b;
+    std::vector<float> xyz(3 * (size_t)m);
+    for (int64_t t = 0; t < m; ++t) {
+        const int64_t g = P->grid[(size_t)P->wall_grid_pos_[(size_t)(b + t)]];
+        xyz[3 * t] = (float)(g / ((int64_t)d[1] * d[2]));
+        xyz[3 * t + 1] = (float)((g / d[2]) % d[1]);
+        xyz[3 * t + 2] = (float)(g % d[2]);
+    }
+    const lbm_vtu_array arr[1] = {{"WallShearStress", 1, 0, P->h_wss + b}};
+    return lbm_vtu_write(path, (size_t)m, xyz.data(), 1, arr);
+}
+
+void lbm_snapshot_destroy(lbm_snapshot* P) {
+    if (P) snapshot_free(P);
+}
+
 void lbm_sim_destroy(lbm_sim* S) {
     if (!S) return;
     free_graph(S);
     for (void* b : S->buf) if (b) cudaFree(b);
     if (S->chunks) cudaFree(S->chunks);
     if (S->chunks2) cudaFree(S->chunks2);
+    if (S->wall_pos) cudaFree(S->wall_pos);
     if (S->zslots) cudaFree(S->zslots);
     if (S->lists) cudaFree(S->lists);
     if (S->insts) cudaFree(S->insts);

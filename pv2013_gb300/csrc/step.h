@@ -32,4 +32,11 @@ lbm_status launch_pair_f32(int Q, int mode, int ra, const StepArgs& a, int wpb, 
 lbm_status launch_pair_f16s(int Q, int mode, int ra, const StepArgs& a, int wpb, cudaStream_t st);
 lbm_status launch_pair_bf16s(int Q, int mode, int ra, const StepArgs& a, int wpb, cudaStream_t st);
 
+// Wall shear stress of every wall lane (one-node-per-lane chunk table):
+// wss[out_pos] = |mu grad u| from the node velocities u (3 per output
+// position); wall_flag[out_pos] = 1 when wall_flag is not null.
+lbm_status launch_wss(int Q, int ra, const Chunk* chunks, int64_t nchunks, const uint32_t* mmask,
+                      const int32_t* out_pos, const InstParam* insts, const double* u, double* wss,
+                      uint8_t* wall_flag, cudaStream_t st);
+
 }  // namespace lbm

@@ -381,6 +381,83 @@ class Simulation:
     def set_divergence_tolerance(self, tol):
         check(load().lbm_sim_set_divergence_tolerance(self._h, float(tol)))
 
+    def wall_shear_stress(self):
+        """Wall shear stress at every wall node, wall-list order (ComputeWallShearStress)."""
+        lib = load()
+        n = C.c_size_t()
+        check(lib.lbm_sim_wall_shear_stress(self._h, None, 0, C.byref(n), self._stream))
+        out = np.empty(n.value)
+        check(lib.lbm_sim_wall_shear_stress(self._h, out.ctypes.data_as(C.c_void_p), out.size, C.byref(n),
+                                            self._stream))
+        return out
+
+    # the reference's names (Simulation.cpp:1374-1421)
+    def ComputeWallShearStress(self):
+        return self.wall_shear_stress()
+
+
+class Snapshot:
+    """Asynchronous snapshot of a simulation (rho, u and/or wall shear stress):
+    capture() enqueues the device work and the copy to pinned host memory and
+    returns; wait() / data() / write_*_vtu() wait for the copy."""
+
+    def __init__(self, sim, fields=True, wss=True):
+        what = (_capi.SNAP_FIELDS if fields else 0) | (_capi.SNAP_WSS if wss else 0)
+        h = C.c_void_p()
+        check(load().lbm_snapshot_create(sim._h, what, C.byref(h)))
+        self._h, self._sim = h, sim
+
+    def capture(self):
+        check(load().lbm_snapshot_capture(self._h, self._sim._stream))
+
+    def wait(self):
+        check(load().lbm_snapshot_wait(self._h))
+
+    def data(self):
+        """(rho, u, wss, step) copies of the last capture (None for fields not captured)."""
+        r, u, w = C.POINTER(C.c_double)(), C.POINTER(C.c_double)(), C.POINTER(C.c_double)()
+        n, nw, step = C.c_size_t(), C.c_size_t(), C.c_int64()
+        check(load().lbm_snapshot_data(self._h, C.byref(r), C.byref(u), C.byref(w), C.byref(n), C.byref(nw),
+                                       C.byref(step)))
+        take = lambda p, k: np.ctypeslib.as_array(p, shape=(k,)).copy() if p else None  # noqa: E731
+        rho = take(r, n.value)
+        vel = take(u, 3 * n.value)
+        return rho, None if vel is None else vel.reshape(-1, 3), take(w, nw.value), step.value
+
+    def write_fields_vtu(self, path, instance=0):
+        check(load().lbm_snapshot_write_fields_vtu(self._h, str(path).encode(), int(instance)))
+
+    def write_wss_vtu(self, path, instance=0):
+        check(load().lbm_snapshot_write_wss_vtu(self._h, str(path).encode(), int(instance)))
+
+    def close(self):
+        if getattr(self, "_h", None):
+            load().lbm_snapshot_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def write_vtu(path, points, arrays):
+    """Point-data .vtu file: points (n, 3); arrays: {name: (n,) or (n, k) float64}."""
+    pts = np.ascontiguousarray(points, dtype=np.float32).reshape(-1, 3)
+    keep, specs = [], []
+    for name, a in arrays.items():
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        keep.append(a)
+        v = _capi.VtuArray()
+        v.name = name.encode()
+        v.components = 1 if a.ndim == 1 else a.shape[1]
+        v.data = a.ctypes.data_as(C.POINTER(C.c_double))
+        specs.append(v)
+    arr = (_capi.VtuArray * max(len(specs), 1))(*specs)
+    check(load().lbm_vtu_write(str(path).encode(), len(pts), pts.ctypes.data_as(C.c_void_p), len(specs),
+                               C.cast(arr, C.c_void_p)))
+
 
 def synth_cylinder(radius, length, segments, axis, center):
     lib = load()
