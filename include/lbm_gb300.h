@@ -312,6 +312,15 @@ typedef struct lbm_monitors {
 } lbm_monitors;
 /* Computes the monitors of the current state (FP64 device reductions). */
 lbm_status lbm_sim_monitors(lbm_sim* s, lbm_monitors* out, void* stream);
+/* Checkpoint / restart: the current populations and step count, written to
+ * a file; lbm_sim_restart loads one into a handle built from the same
+ * geometry and parameters (checked: lattice size, storage, pattern and a hash
+ * of the node positions), after which stepping continues exactly as it would
+ * have from the checkpointed state.  Replaces nothing in the reference (it
+ * has no restart); writes whole files, synchronises the stream. */
+lbm_status lbm_sim_checkpoint(lbm_sim* s, const char* path, void* stream);
+lbm_status lbm_sim_restart(lbm_sim* s, const char* path, void* stream);
+
 /* Divergence monitor used with LBM_STEP_MONITOR: the step call returns
  * LBM_ERR_DIVERGED when a value is non-finite or |mass/mass0 - 1| > rel_tol. */
 lbm_status lbm_sim_set_divergence_tolerance(lbm_sim* s, double rel_tol);

@@ -131,6 +131,8 @@ PROTOTYPES = {
     "lbm_snapshot_write_fields_vtu": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int32]),
     "lbm_snapshot_write_wss_vtu": (C.c_int, [C.c_void_p, C.c_char_p, C.c_int32]),
     "lbm_snapshot_destroy": (None, [C.c_void_p]),
+    "lbm_sim_checkpoint": (C.c_int, [C.c_void_p, C.c_char_p, C.c_void_p]),
+    "lbm_sim_restart": (C.c_int, [C.c_void_p, C.c_char_p, C.c_void_p]),
     "lbm_sim_nodes": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "lbm_sim_instance_offsets": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "lbm_sim_monitors": (C.c_int, [C.c_void_p, _P(Monitors), C.c_void_p]),

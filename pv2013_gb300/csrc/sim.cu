@@ -1587,6 +1587,102 @@ void lbm_snapshot_destroy(lbm_snapshot* P) {
     if (P) snapshot_free(P);
 }
 
+// Checkpoint file: a fixed header, then the populations of the current state
+// (the plane-major device array, stride * Q values of the storage type).
+namespace {
+struct CkptHeader {
+    char magic[8];            // "LBMCKPT1"
+    int32_t Q, store, pattern, n_inst;
+    int64_t N, NF, stride, nchunks, steps_done;
+    uint64_t grid_hash;       // FNV-1a of the output nodes' grid indices
+    uint64_t bytes;
+};
+uint64_t fnv1a(const void* p, size_t n, uint64_t h = 1469598103934665603ull) {
+    const unsigned char* c = (const unsigned char*)p;
+    for (size_t i = 0; i < n; ++i) { h ^= c[i]; h *= 1099511628211ull; }
+    return h;
+}
+lbm_status ckpt_header(lbm_sim* S, CkptHeader& h) {
+    std::memset(&h, 0, sizeof h);
+    std::memcpy(h.magic, "LBMCKPT1", 8);
+    h.Q = S->Q; h.store = S->store; h.pattern = S->pattern; h.n_inst = (int32_t)S->n_inst;
+    h.N = S->N; h.NF = S->NF; h.stride = S->stride; h.nchunks = S->nchunks; h.steps_done = S->steps_done;
+    std::vector<int64_t> g((size_t)S->NF);
+    LBM_CUDA(cudaMemcpy(g.data(), S->node_grid, sizeof(int64_t) * S->NF, cudaMemcpyDeviceToHost));
+    h.grid_hash = fnv1a(g.data(), g.size() * sizeof(int64_t));
+    h.bytes = (uint64_t)S->stride * S->Q * store_bytes(S->store);
+    return LBM_OK;
+}
+constexpr size_t kCkptBlock = size_t(64) << 20;
+}  // namespace
+
+lbm_status lbm_sim_checkpoint(lbm_sim* S, const char* path, void* stream) {
+    if (!S || !path) return fail(LBM_ERR_ARG, "lbm_sim_checkpoint: null argument");
+    clear_error();
+    cudaStream_t st = (cudaStream_t)stream;
+    LBM_TRY(check_timeout(S, st));         // also orders the state after the caller's work
+    CkptHeader h;
+    LBM_TRY(ckpt_header(S, h));
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return fail(LBM_ERR_IO, "cannot open %s for writing", path);
+    bool ok = std::fwrite(&h, sizeof h, 1, f) == 1;
+    const char* src = (const char*)S->buf[S->pattern == LBM_PULL ? S->cur : 0];
+    std::vector<char> blk(std::min<size_t>(kCkptBlock, (size_t)h.bytes));
+    for (uint64_t off = 0; ok && off < h.bytes; off += blk.size()) {
+        const size_t n = (size_t)std::min<uint64_t>(blk.size(), h.bytes - off);
+        if (cudaMemcpy(blk.data(), src + off, n, cudaMemcpyDeviceToHost) != cudaSuccess) {
+            std::fclose(f);
+            return fail(LBM_ERR_CUDA, "checkpoint: device copy failed");
+        }
+        ok = std::fwrite(blk.data(), 1, n, f) == n;
+    }
+    ok = (std::fclose(f) == 0) && ok;
+    if (!ok) return fail(LBM_ERR_IO, "writing %s failed", path);
+    return LBM_OK;
+}
+
+lbm_status lbm_sim_restart(lbm_sim* S, const char* path, void* stream) {
+    if (!S || !path) return fail(LBM_ERR_ARG, "lbm_sim_restart: null argument");
+    clear_error();
+    cudaStream_t st = (cudaStream_t)stream;
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return fail(LBM_ERR_IO, "cannot open %s", path);
+    CkptHeader h, mine;
+    const bool got = std::fread(&h, sizeof h, 1, f) == 1;
+    lbm_status hs = ckpt_header(S, mine);
+    if (hs != LBM_OK) { std::fclose(f); return hs; }
+    if (!got || std::memcmp(h.magic, "LBMCKPT1", 8) != 0) {
+        std::fclose(f);
+        return fail(LBM_ERR_PARSE, "%s is not a checkpoint of this engine", path);
+    }
+    if (h.Q != mine.Q || h.store != mine.store || h.pattern != mine.pattern || h.n_inst != mine.n_inst ||
+        h.N != mine.N || h.NF != mine.NF || h.stride != mine.stride || h.nchunks != mine.nchunks ||
+        h.grid_hash != mine.grid_hash || h.bytes != mine.bytes) {
+        std::fclose(f);
+        return fail(LBM_ERR_ARG, "%s was written for another lattice or storage (Q %d/%d, precision %d/%d, pattern "
+                                 "%d/%d, nodes %lld/%lld)", path, h.Q, mine.Q, h.store, mine.store, h.pattern,
+                    mine.pattern, (long long)h.N, (long long)mine.N);
+    }
+    LBM_CUDA(cudaStreamSynchronize(st));
+    char* dst = (char*)S->buf[0];
+    std::vector<char> blk(std::min<size_t>(kCkptBlock, (size_t)h.bytes));
+    for (uint64_t off = 0; off < h.bytes; off += blk.size()) {
+        const size_t n = (size_t)std::min<uint64_t>(blk.size(), h.bytes - off);
+        if (std::fread(blk.data(), 1, n, f) != n) {
+            std::fclose(f);
+            return fail(LBM_ERR_PARSE, "%s is truncated", path);
+        }
+        if (cudaMemcpy(dst + off, blk.data(), n, cudaMemcpyHostToDevice) != cudaSuccess) {
+            std::fclose(f);
+            return fail(LBM_ERR_CUDA, "restart: device copy failed");
+        }
+    }
+    std::fclose(f);
+    S->cur = 0;
+    S->steps_done = h.steps_done;
+    return LBM_OK;
+}
+
 void lbm_sim_destroy(lbm_sim* S) {
     if (!S) return;
     free_graph(S);

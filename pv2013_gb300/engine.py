@@ -391,6 +391,14 @@ class Simulation:
                                             self._stream))
         return out
 
+    def checkpoint(self, path):
+        """Writes the current populations and step count to a file."""
+        check(load().lbm_sim_checkpoint(self._h, str(path).encode(), self._stream))
+
+    def restart(self, path):
+        """Loads a checkpoint written by a simulation of the same lattice and parameters."""
+        check(load().lbm_sim_restart(self._h, str(path).encode(), self._stream))
+
     # the reference's names (Simulation.cpp:1374-1421)
     def ComputeWallShearStress(self):
         return self.wall_shear_stress()

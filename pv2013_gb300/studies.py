@@ -2,6 +2,7 @@
 
     python -m pv2013_gb300.studies precision --case bifurcation --Q 27 --taus 0.51,0.55,0.8 --steps 10000
     python -m pv2013_gb300.studies ensemble --n 64 --steps 2000
+    python -m pv2013_gb300.studies pv2013 --steps 20000 [--stl PV2013.stl]
 
 precision: for each relaxation time, the FP64 run (the reference's
 arithmetic, bit-exact with the CPU oracle) and the FP32 / FP16-shifted /
@@ -18,6 +19,10 @@ amplitude and period) advance together in one launch per step over a packed
 node list (FP16-shifted storage, AA pattern, CUDA-graph replay, autotuned
 kernel); the study reports the aggregate MLUPS and, for a subset, the
 per-instance velocity error against FP64 runs of the same instances.
+
+pv2013: the reference's own production run (PV2013 geometry, spacing 0.1,
+tau 0.66, 20 000 iterations) in FP64 (the reference's arithmetic) and
+FP16-shifted storage, timed against the reference's recorded run.
 
 Prints one JSON object.
 """
@@ -140,6 +145,66 @@ def ensemble_study(n, steps, check=4, check_steps=500):
             "error_vs_fp64": {"steps": check_steps, "per_instance": errs}}
 
 
+# The reference's production run (slurm-427156.out): PV2013.stl at spacing
+# 0.1, tau 0.66, 20 000 iterations on one rank: 71 568.30 s in total, about
+# 2 942 s of set-up and a median of 3.34 s per iteration without output.
+REF_PV2013_TOTAL_S = 71568.30
+REF_PV2013_SETUP_S = 2942.0
+REF_PV2013_STEP_S = 3.34
+
+
+def pv2013_study(tris, steps, precisions=("f64", "f16s"), output_every=0, outdir=None):
+    """The reference's own run: PV2013 geometry (its seven predicate lists),
+    spacing 0.1, tau 0.66, velocity inlet (0, -0.1, 0), outlets at rho 1.01."""
+    import torch
+    from .engine import pv2013_predicates
+    out = {"case": "PV2013", "steps": steps, "reference": {"total_s": REF_PV2013_TOTAL_S, "setup_s": REF_PV2013_SETUP_S,
+                                                          "step_s": REF_PV2013_STEP_S}, "runs": {}}
+    torch.cuda.synchronize()
+    t0 = time.time()
+    geom = Geometry(tris, 0.1, predicates=pv2013_predicates())
+    torch.cuda.synchronize()
+    out["geometry_s"] = time.time() - t0
+    out["voxelize_ms"] = geom.info.voxelize_ms
+    out["dims"] = list(geom.GeomSize)
+    out["fluid_nodes"] = geom.info.n_fluid
+    kinds = [_capi.BC_VEL_NEGY, _capi.BC_PRESS_NEGY, _capi.BC_PRESS_POSY, _capi.BC_PRESS_POSX, _capi.BC_PRESS_POSX,
+             _capi.BC_PRESS_POSX, _capi.BC_PRESS_POSZ]
+    specs = [BoundarySpec(0, kinds[0], dir=(0.0, -1.0, 0.0), amp=np.array([0.1]))]
+    specs += [BoundarySpec(l, kinds[l], rho=1.01) for l in range(1, 7)]
+    for prec in precisions:
+        t0 = time.time()
+        sim = Simulation(geom, 0.66, specs, precision=prec, pattern="pull" if prec == "f64" else "aa")
+        torch.cuda.synchronize()
+        t_build = time.time() - t0
+        snap = None
+        if output_every and outdir:
+            import os
+            from .engine import Snapshot
+            os.makedirs(outdir, exist_ok=True)
+            snap = Snapshot(sim, fields=True, wss=True)
+        t0 = time.time()
+        done = 0
+        while done < steps:
+            k = min(output_every or steps, steps - done)
+            sim.step(k, graph=True)
+            done += k
+            if snap is not None:
+                snap.capture()
+                snap.write_fields_vtu(f"{outdir}/{prec}_{done}.vtu")
+                snap.write_wss_vtu(f"{outdir}/{prec}_{done}_wall_shear_stress.vtu")
+        torch.cuda.synchronize()
+        sec = time.time() - t0
+        mon = sim.monitors()
+        out["runs"][prec] = {"lattice_build_s": t_build, "steps_s": sec, "ms_per_step": sec / steps * 1e3,
+                             "mlups": geom.info.n_fluid * steps / sec / 1e6,
+                             "speedup_per_step_vs_reference": REF_PV2013_STEP_S / (sec / steps),
+                             "total_s": out["geometry_s"] + t_build + sec,
+                             "mass": mon["mass"], "max_speed": mon["max_speed"], "nonfinite": mon["nonfinite"]}
+        del sim
+    return out
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(prog="python -m pv2013_gb300.studies")
     sub = ap.add_subparsers(dest="study", required=True)
@@ -149,6 +214,11 @@ def main(argv=None):
     p.add_argument("--taus", default="0.6")
     p.add_argument("--steps", type=int, default=10000)
     p.add_argument("--h", type=float, default=None)
+    v = sub.add_parser("pv2013")
+    v.add_argument("--stl", help="PV2013.stl (ASCII); default: the triangles of tests/golden/pv2013_tris.npz")
+    v.add_argument("--steps", type=int, default=20000)
+    v.add_argument("--output-every", type=int, default=0)
+    v.add_argument("--outdir", default=None)
     e = sub.add_parser("ensemble")
     e.add_argument("--n", type=int, default=64)
     e.add_argument("--steps", type=int, default=2000)
@@ -160,6 +230,16 @@ def main(argv=None):
         kw = {"h": a.h} if a.h else ({"h": 2.2} if a.case == "vascular_tree" else {})
         case = maker(**kw)
         res = precision_study(case, a.Q, [float(t) for t in a.taus.split(",")], a.steps)
+    elif a.study == "pv2013":
+        from .engine import Reader
+        if a.stl:
+            tris = Reader.readSTLASCII(a.stl)
+        else:
+            import os
+            fx = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "tests", "golden",
+                              "pv2013_tris.npz")
+            tris = np.load(fx)["tris"]
+        res = pv2013_study(tris, a.steps, output_every=a.output_every, outdir=a.outdir)
     else:
         res = ensemble_study(a.n, a.steps)
     print(json.dumps(res))

@@ -77,3 +77,40 @@ def test_snapshot_is_the_captured_state(tmp_path):
     _, nw, w = T._read_vtu(tmp_path / "w.vtu")
     assert nw == len(geom.WallboundaryPoints)
     snap.close()
+
+
+@pytest.mark.parametrize("precision,pattern", [("f64", "pull"), ("f64", "aa"), ("f16s", "aa"), ("f32", "pull")])
+def test_checkpoint_restart_continues_exactly(tmp_path, precision, pattern):
+    c = cases.vessel(4001)
+    geom = c.geometry()
+    a = Simulation(geom, c.tau, c.boundary_specs(geom), precision=precision, pattern=pattern)
+    a.step(21)                                        # odd: AA parity and pull buffer index matter
+    a.checkpoint(tmp_path / "s.ckpt")
+    a.step(30, graph=True)
+    b = Simulation(geom, c.tau, c.boundary_specs(geom), precision=precision, pattern=pattern)
+    b.restart(tmp_path / "s.ckpt")
+    assert b.info().steps_done == 21
+    b.step(30, graph=True)
+    assert np.array_equal(a.fields()[0], b.fields()[0])
+
+
+def test_restart_rejects_other_lattices(tmp_path):
+    from pv2013_gb300 import _capi
+    c1, c2 = cases.vessel(4001), cases.vessel(4002)
+    g1, g2 = c1.geometry(), c2.geometry()
+    a = Simulation(g1, c1.tau, c1.boundary_specs(g1), precision="f32", pattern="aa")
+    a.checkpoint(tmp_path / "a.ckpt")
+    b = Simulation(g2, c2.tau, c2.boundary_specs(g2), precision="f32", pattern="aa")
+    with pytest.raises(_capi.LbmError) as e:
+        b.restart(tmp_path / "a.ckpt")
+    assert e.value.status == _capi.ERR_ARG
+    c = Simulation(g1, c1.tau, c1.boundary_specs(g1), precision="f16s", pattern="aa")
+    with pytest.raises(_capi.LbmError):
+        c.restart(tmp_path / "a.ckpt")
+    (tmp_path / "junk.ckpt").write_bytes(b"not a checkpoint")
+    with pytest.raises(_capi.LbmError) as e:
+        a.restart(tmp_path / "junk.ckpt")
+    assert e.value.status == 2
+    with pytest.raises(_capi.LbmError) as e:
+        a.restart(tmp_path / "missing.ckpt")
+    assert e.value.status == 1
