@@ -358,12 +358,12 @@ __global__ void __launch_bounds__(256, PairMinBlocks<Q, S, MODE>::value) k_step2
                 const bool dir_ok = q != L::NO_BB_POP || all_dirs;
                 const bool bl = ml && w_lo && dir_ok, bh = mh && w_hi && dir_ok;
                 if constexpr (MODE != MODE_AA_EVEN) {
-                    // bounce-back source: own node, slot opp(q) (pull) or slot q (AA odd)
-                    if (bl || bh) {
-                        const W own = ldw<S>(A, (uint32_t)(MODE == MODE_PULL ? L::opp(q) : q) * st + e);
-                        if (bl) raw[q] = take_half<S>(raw[q], false, own);
-                        if (bh) raw[q] = take_half<S>(raw[q], true, own);
-                    }
+                    // bounce-back source: own node, slot opp(q) (pull) or slot q (AA
+                    // odd); a predicated load and selects instead of branches
+                    W own = raw[q];
+                    if (bl || bh) own = ldw<S>(A, (uint32_t)(MODE == MODE_PULL ? L::opp(q) : q) * st + e);
+                    raw[q] = take_half<S>(raw[q], false, bl ? own : raw[q]);
+                    raw[q] = take_half<S>(raw[q], true, bh ? own : raw[q]);
                 }
                 // AA even: slot q of x already holds f*_{opp q}(x)
                 if (ml && !bl) raw[q] = init_half<S, Q>(raw[q], false, q);
