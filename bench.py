@@ -113,6 +113,16 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
+def max_over_ranks(x, world, device):
+    """The largest value over the ranks (the slowest replica's time)."""
+    if world <= 1:
+        return x
+    import torch
+    t = torch.tensor([float(x)], device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
 def time_steps(sim, steps, warmup, torch):
     sim.step(warmup, graph=True)
     torch.cuda.synchronize()
@@ -220,10 +230,7 @@ def gpu_arm(args, rank, world):
         if world > 1:
             torch.distributed.barrier()
         sec16 = time_steps(sim16, args.steps, args.warmup, torch)
-    if world > 1:
-        t = torch.tensor([sec16], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        sec16 = float(t.item())
+    sec16 = max_over_ranks(sec16, world, "cuda")
     mon = sim16.monitors()
     ms_step = sec16 / args.steps * 1e3
     mlups16 = nf * args.steps / sec16 / 1e6 * world
@@ -233,12 +240,12 @@ def gpu_arm(args, rank, world):
     # --- plain FP32 two-lattice pull: one node per lane, direct loads --------
     sim32 = Simulation(geom, case.tau, specs, precision="f32", pattern="pull", run_axis=0, staging=1,
                        nodes_per_lane=1)
-    sec32 = time_steps(sim32, args.steps, args.warmup, torch)
+    sec32 = max_over_ranks(time_steps(sim32, args.steps, args.warmup, torch), world, "cuda")
     mlups32 = nf * args.steps / sec32 / 1e6 * world
     del sim32
     # the same FP32 two-lattice pull through the paired kernel, for reference
     sim32p = Simulation(geom, case.tau, specs, precision="f32", pattern="pull", run_axis=0, nodes_per_lane=2)
-    sec32p = time_steps(sim32p, args.steps, args.warmup, torch)
+    sec32p = max_over_ranks(time_steps(sim32p, args.steps, args.warmup, torch), world, "cuda")
     mlups32p = nf * args.steps / sec32p / 1e6 * world
     del sim32p
 
@@ -286,7 +293,7 @@ def gpu_arm(args, rank, world):
         esim = Simulation(egeo, [c.tau for c in ens], [c.boundary_specs(g) for c, g in zip(ens, egeo)],
                           precision="f16s", pattern=args.pattern)
         esim.autotune(launches=10)
-        esec = time_steps(esim, args.batch_steps, args.warmup, torch)
+        esec = max_over_ranks(time_steps(esim, args.batch_steps, args.warmup, torch), world, "cuda")
         einfo = esim.info()
         batched = {"workload": "ensemble of 64 tortuous vessels (seeds 4000-4063), per-instance tau, inlet amplitude "
                                "and period, FP16-shifted AA, one launch per step",
