@@ -256,17 +256,17 @@ __device__ __forceinline__ void collide2(const typename PairWord<S>::W* raw, flo
     }
 }
 
-// register budget per thread: D3Q19 with 16-bit storage holds one 32-bit
-// word per population: 64 registers (4 blocks of 256; measured faster than 80
-// registers for the AA odd pattern, whose occupancy matters more than its few
-// spilled values); FP32 storage (two registers per word) and D3Q27 get 128
-// (2 blocks)
-template <int Q, int S, int MODE> struct PairMinBlocks {
-    static constexpr int value = (Q == 19 && S != ST_F32) ? 4 : 2;
+// register budget per thread (measured on the vascular tree): D3Q19 with
+// 16-bit storage holds one 32-bit word per population; 64 registers for the
+// node-local and pull patterns, 72 for the AA odd pattern (its scatter needs a
+// few more; 72 keeps 28 warps per SM and removes the spills of a 64 budget);
+// FP32 storage (two registers per word) and D3Q27 get 128.
+template <int Q, int S, int MODE> struct PairMaxReg {
+    static constexpr int value = (Q == 19 && S != ST_F32) ? (MODE == MODE_AA_ODD ? 72 : 64) : 128;
 };
 
 template <int Q, int S, int MODE, int RA>
-__global__ void __launch_bounds__(256, PairMinBlocks<Q, S, MODE>::value) k_step2(StepArgs a) {
+__global__ void __launch_bounds__(256) __maxnreg__((PairMaxReg<Q, S, MODE>::value)) k_step2(StepArgs a) {
     using L = Lat<Q>;
     using X = Ax<Q, RA>;
     using W = typename PairWord<S>::W;
