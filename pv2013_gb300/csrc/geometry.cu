@@ -77,10 +77,22 @@ __device__ bool enumerate_columns(const VoxGrid& g, const double* T, F fn) {
     const int pad = 2 + (int)ceil(0.01 / s);
     const double xmn = fmin(T[0], fmin(T[3], T[6])), xmx = fmax(T[0], fmax(T[3], T[6]));
     const double ymn = fmin(T[1], fmin(T[4], T[7])), ymx = fmax(T[1], fmax(T[4], T[7]));
-    long i0 = (long)floor((xmn - g.bb[0]) / s) - pad, i1 = (long)ceil((xmx - g.bb[0]) / s) + pad;
-    long j0 = (long)floor((ymn - g.bb[2]) / s) - pad, j1 = (long)ceil((ymx - g.bb[2]) / s) + pad;
-    i0 = max(i0, 0L); j0 = max(j0, 0L);
-    i1 = min(i1, (long)g.Nx - 1); j1 = min(j1, (long)g.Ny - 1);
+    // columns whose ray (min + i*s, nudged by at most 0.01 at the grid faces)
+    // lies within 0.01 of the projection's bounding box: a non-degenerate
+    // triangle contains no point outside its box, and the margin covers the
+    // face nudge; the bounds are found with the same expression column_xy uses
+    auto lower = [&](double v, double base, int n) -> long {   // first i with base + i*s >= v
+        long i = max((long)floor((v - base) / s) - 1, 0L);
+        while (i < n && base + (double)i * s < v) ++i;
+        return i;
+    };
+    auto upper = [&](double v, double base, int n) -> long {   // last i with base + i*s <= v
+        long i = min((long)ceil((v - base) / s) + 1, (long)n - 1);
+        while (i >= 0 && base + (double)i * s > v) --i;
+        return i;
+    };
+    const long i0 = lower(xmn - 0.01, g.bb[0], g.Nx), i1 = upper(xmx + 0.01, g.bb[0], g.Nx);
+    const long j0 = lower(ymn - 0.01, g.bb[2], g.Ny), j1 = upper(ymx + 0.01, g.bb[2], g.Ny);
     double ex[3] = {T[3] - T[0], T[6] - T[3], T[0] - T[6]};
     double ey[3] = {T[4] - T[1], T[7] - T[4], T[1] - T[7]};
     int e = 0;

@@ -125,26 +125,55 @@ struct Pad {
     __host__ __device__ int64_t cell(int64_t a, int64_t b, int64_t r) const { return (a * Pb() + b) * Pr() + r; }
 };
 
-__global__ void k_types(const uint8_t* __restrict__ pflags, Pad D, uint8_t* __restrict__ type) {
-    const int64_t n = D.cells();
-    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t r = c % D.Pr(), t = c / D.Pr();
-        const int64_t b = t % D.Pb(), a = t / D.Pb();
-        auto fluid = [&](int64_t aa, int64_t bb, int64_t rr) {
-            return aa >= 1 && aa <= D.Na && bb >= 1 && bb <= D.Nb && rr >= 1 && rr <= D.Nr &&
-                   pflags[((aa - 1) * D.Nb + (bb - 1)) * D.Nr + (rr - 1)] != 0;
-        };
-        uint8_t ty = 0;
-        if (fluid(a, b, r)) {
-            ty = 2;
-        } else {
-            for (int da = -1; da <= 1 && !ty; ++da)
-                for (int db = -1; db <= 1 && !ty; ++db)
-                    for (int dr = -1; dr <= 1 && !ty; ++dr)
-                        if (fluid(a + da, b + db, r + dr)) ty = 1;
-        }
-        type[c] = ty;
+// Node types by separable dilation: the 3x3x3 neighbourhood test as three
+// 3-point passes (run axis, b, a), one thread per cell with the coordinates
+// taken from the launch grid.
+__global__ void k_dil_r(const uint8_t* __restrict__ pflags, Pad D, uint8_t* __restrict__ t1) {
+    const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t b = blockIdx.y, a = blockIdx.z;
+    if (r >= D.Pr()) return;
+    uint8_t v = 0;
+    if (a >= 1 && a <= D.Na && b >= 1 && b <= D.Nb) {
+        const uint8_t* col = pflags + ((a - 1) * D.Nb + (b - 1)) * (int64_t)D.Nr;
+        for (int64_t rr = r - 1; rr <= r + 1; ++rr)
+            if (rr >= 1 && rr <= D.Nr && col[rr - 1]) v = 1;
     }
+    t1[D.cell(a, b, r)] = v;
+}
+__global__ void k_dil_b(const uint8_t* __restrict__ t1, Pad D, uint8_t* __restrict__ t2) {
+    const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t b = blockIdx.y, a = blockIdx.z;
+    if (r >= D.Pr()) return;
+    uint8_t v = 0;
+    for (int64_t bb = b - 1; bb <= b + 1; ++bb)
+        if (bb >= 0 && bb < D.Pb()) v |= t1[D.cell(a, bb, r)];
+    t2[D.cell(a, b, r)] = v;
+}
+__global__ void k_dil_a(const uint8_t* __restrict__ t2, const uint8_t* __restrict__ pflags, Pad D,
+                        uint8_t* __restrict__ type) {
+    const int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    const int64_t b = blockIdx.y, a = blockIdx.z;
+    if (r >= D.Pr()) return;
+    uint8_t v = 0;
+    for (int64_t aa = a - 1; aa <= a + 1; ++aa)
+        if (aa >= 0 && aa < D.Pa()) v |= t2[D.cell(aa, b, r)];
+    const bool fluid = a >= 1 && a <= D.Na && b >= 1 && b <= D.Nb && r >= 1 && r <= D.Nr &&
+                       pflags[((a - 1) * D.Nb + (b - 1)) * (int64_t)D.Nr + (r - 1)] != 0;
+    type[D.cell(a, b, r)] = fluid ? 2 : (v ? 1 : 0);
+}
+
+// type of every padded cell (2 fluid, 1 ghost, 0 none); scratch: one more
+// byte per cell
+lbm_status compute_types(const uint8_t* pflags, const Pad& D, uint8_t* type, cudaStream_t st) {
+    DBuf<uint8_t> tmp;
+    LBM_TRY(tmp.alloc(D.cells(), "node type scratch"));
+    const dim3 grid((unsigned)((D.Pr() + 255) / 256), (unsigned)D.Pb(), (unsigned)D.Pa());
+    k_dil_r<<<grid, 256, 0, st>>>(pflags, D, type);
+    k_dil_b<<<grid, 256, 0, st>>>(type, D, tmp.p);
+    k_dil_a<<<grid, 256, 0, st>>>(tmp.p, pflags, D, type);
+    LBM_CUDA(cudaGetLastError());
+    LBM_CUDA(cudaStreamSynchronize(st));   // the scratch is freed on return
+    return LBM_OK;
 }
 
 // Extra ghost nodes so that every node id has the parity of its level: one
@@ -558,7 +587,7 @@ lbm_status count_chunks(const lbm_geometry* g, int ra, cudaStream_t st, int64_t*
     const Pad D{P.Na(), P.Nb(), P.Nr()};
     DBuf<uint8_t> type;
     LBM_TRY(type.alloc(D.cells(), "node types"));
-    k_types<<<blocks_for(D.cells(), 256), 256, 0, st>>>(flags, D, type.p);
+    LBM_TRY(compute_types(flags, D, type.p, st));
     // chunks only depend on the fluid runs; roles are not needed: count with
     // a role array of zeros via the fluid cells themselves
     const int64_t ncol = (int64_t)D.Na * D.Nb;
@@ -596,7 +625,7 @@ lbm_status build_instance(const lbm_geometry* g, const lbm_sim_params* p, int Q,
     const Pad D{P.Na(), P.Nb(), P.Nr()};
     DBuf<uint8_t> type;
     LBM_TRY(type.alloc(D.cells(), "node types"));
-    k_types<<<blocks_for(D.cells(), 256), 256, 0, st>>>(pflags, D, type.p);
+    LBM_TRY(compute_types(pflags, D, type.p, st));
     k_parity_ghosts<<<blocks_for(D.cells(), 256), 256, 0, st>>>(D, type.p);
     int64_t* nc = nullptr;
     LBM_TRY(scan::compact(type.p, D.cells(), &nc, &out.N, st));
