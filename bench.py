@@ -224,7 +224,7 @@ def gpu_arm(args, rank, world):
 
     # --- headline: FP16-shifted storage, AA in-place streaming ---------------
     sim16 = Simulation(geom, case.tau, specs, precision="f16s", pattern=args.pattern, run_axis=0,
-                       staging=args.staging, nodes_per_lane=args.nodes_per_lane)
+                       staging=args.staging, nodes_per_lane=args.nodes_per_lane, piece_slots=args.piece_slots)
     info16 = sim16.info()
     with ClockSampler(dev) as clk:
         if world > 1:
@@ -257,7 +257,7 @@ def gpu_arm(args, rank, world):
     m64 = s64.monitors()["mass"]
     del s64
     s16 = Simulation(geom, case.tau, specs, precision="f16s", pattern=args.pattern, run_axis=0, staging=args.staging,
-                     nodes_per_lane=args.nodes_per_lane)
+                     nodes_per_lane=args.nodes_per_lane, piece_slots=args.piece_slots)
     m0 = s16.monitors()["mass"]
     s16.step(err_steps, graph=True)
     _, r16, u16 = s16.fields(f=False)
@@ -274,7 +274,7 @@ def gpu_arm(args, rank, world):
     t0 = time.time()
     g2 = case.geometry()
     s2 = Simulation(g2, case.tau, case.boundary_specs(g2), precision="f16s", pattern=args.pattern, run_axis=0,
-                    staging=args.staging, nodes_per_lane=args.nodes_per_lane)
+                    staging=args.staging, nodes_per_lane=args.nodes_per_lane, piece_slots=args.piece_slots)
     s2.step(e2e_steps, graph=True)
     _, rho_h, u_h = s2.fields(f=False)
     torch.cuda.synchronize()
@@ -291,7 +291,7 @@ def gpu_arm(args, rank, world):
         egeo = [c.geometry() for c in ens]
         enf = sum(g.info.n_fluid for g in egeo)
         esim = Simulation(egeo, [c.tau for c in ens], [c.boundary_specs(g) for c, g in zip(ens, egeo)],
-                          precision="f16s", pattern=args.pattern)
+                          precision="f16s", pattern=args.pattern, piece_slots=args.piece_slots)
         esim.autotune(launches=10)
         esec = max_over_ranks(time_steps(esim, args.batch_steps, args.warmup, torch), world, "cuda")
         einfo = esim.info()
@@ -299,7 +299,8 @@ def gpu_arm(args, rank, world):
                                "and period, FP16-shifted AA, one launch per step",
                    "fluid_nodes": enf, "steps": args.batch_steps, "mlups": enf * args.batch_steps / esec / 1e6 * world,
                    "ms_per_step": esec / args.batch_steps * 1e3,
-                   "kernel": {"nodes_per_lane": einfo.nodes_per_lane, "warps_per_block": einfo.warps_per_block}}
+                   "kernel": {"nodes_per_lane": einfo.nodes_per_lane, "piece_slots": einfo.piece_slots,
+                              "warps_per_block": einfo.warps_per_block}}
         del esim, egeo
 
     # --- roofline of the step kernel ------------------------------------------
@@ -334,7 +335,8 @@ def gpu_arm(args, rank, world):
                    "precision": "f16s", "pattern": args.pattern, "run_axis": info16.run_axis,
                    "kernel": ("paired: 2 nodes/lane, f32x2 math" if info16.nodes_per_lane == 2 else
                               "1 node/lane, " + ("tma-staged" if args.staging == 0 else "direct loads")),
-                   "warps_per_block": info16.warps_per_block, "chunks": info16.n_chunks,
+                   "piece_slots": info16.piece_slots, "warps_per_block": info16.warps_per_block,
+                   "chunks": info16.n_chunks,
                    "l2": "populations exceed L2 (no flush needed)", "parallelism": f"replicas x{world}"},
         "fp32_pull_mlups": mlups32, "f16_over_f32": mlups16 / mlups32,
         "fp32_pull_plain": "FP32 storage and math, two-lattice pull, one node per lane, direct loads",
@@ -362,6 +364,8 @@ def main():
     ap.add_argument("--pattern", default="aa", choices=["aa", "pull"])
     ap.add_argument("--staging", type=int, default=1, help="0 = TMA-staged pipeline, 1 = direct loads")
     ap.add_argument("--nodes-per-lane", type=int, default=0, help="0 = engine default (paired), 1 or 2")
+    ap.add_argument("--piece-slots", type=int, default=0, help="paired kernel: 8, 16 or 32 node slots per chunk "
+                                                                   "piece; 0 = engine default (16)")
     ap.add_argument("--err-steps", type=int, default=500)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-vessel ensemble line")

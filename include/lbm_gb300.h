@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define LBM_ABI_VERSION 2
+#define LBM_ABI_VERSION 3
 
 typedef enum lbm_status {
     LBM_OK = 0,
@@ -230,6 +230,11 @@ typedef struct lbm_sim_params {
                                   LBM_FIX_LIST_NODES: bounce back the missing populations of
                                     inlet/outlet nodes before their Zou-He routine (the
                                     reference leaves them at their initial value) */
+    int32_t piece_slots;       /* two nodes per lane: node slots per chunk piece (8, 16 or 32;
+                                  a piece is one run segment served by piece_slots/2 lanes,
+                                  so shorter pieces leave fewer idle lanes at run ends and
+                                  read more descriptor bytes); 0 = default (16).  Results do
+                                  not depend on it. */
 } lbm_sim_params;
 
 #define LBM_FIX_BB_ALL_DIRS 1
@@ -265,7 +270,7 @@ typedef struct lbm_sim_info {
     double algorithmic_bytes_per_update;  /* 2*Q*storage bytes */
     int64_t n_lattice_nodes;   /* fluid + ghost nodes (the population arrays' length) */
     int32_t nodes_per_lane;
-    int32_t reserved;
+    int32_t piece_slots;       /* node slots per chunk piece (two nodes per lane), else 0 */
 } lbm_sim_info;
 lbm_status lbm_sim_info_get(const lbm_sim* s, lbm_sim_info* info);
 

@@ -7,7 +7,8 @@
 The run file uses the reference's ConfigReader format (ConfigReader.cpp:13-51):
 one `key value` pair per line, `#` starts a comment line; command-line options
 override it.  Keys: case, stl, preset, spacing, tau, steps, warmup, precision,
-pattern, Q, u_in, outlet_rho, run_axis, staging, warps_per_block, nodes_per_lane.
+pattern, Q, u_in, outlet_rho, run_axis, staging, warps_per_block, nodes_per_lane,
+piece_slots.
 
 Named cases are the seeded synthetic workloads of pv2013_gb300.cases (pipe,
 pipe_x, bifurcation, vascular_tree, vessel); `--stl FILE --preset pv2013` runs
@@ -25,7 +26,7 @@ import time
 
 KEYS = {"case": str, "stl": str, "preset": str, "spacing": float, "tau": float, "steps": int, "warmup": int,
         "precision": str, "pattern": str, "Q": int, "u_in": float, "outlet_rho": float, "run_axis": int,
-        "staging": int, "warps_per_block": int, "nodes_per_lane": int, "h": float}
+        "staging": int, "warps_per_block": int, "nodes_per_lane": int, "piece_slots": int, "h": float}
 
 
 def read_run_file(path):
@@ -98,7 +99,8 @@ def main(argv=None):
     t0 = time.time()
     sim = Simulation(g, tau, specs, Q=Q, precision=cfg.get("precision", "f64"), pattern=cfg.get("pattern", "pull"),
                      warps_per_block=cfg.get("warps_per_block", 0), run_axis=cfg.get("run_axis", 0),
-                     staging=cfg.get("staging", 1), nodes_per_lane=cfg.get("nodes_per_lane", 0))
+                     staging=cfg.get("staging", 1), nodes_per_lane=cfg.get("nodes_per_lane", 0),
+                     piece_slots=cfg.get("piece_slots", 0))
     torch.cuda.synchronize()
     t_build = time.time() - t0
     steps, warmup = cfg.get("steps", 100), cfg.get("warmup", 3)
@@ -117,7 +119,8 @@ def main(argv=None):
         "case": cfg.get("stl") or cfg.get("case", "pipe"), "Q": info.Q, "precision": cfg.get("precision", "f64"),
         "pattern": cfg.get("pattern", "pull"), "dims": list(g.GeomSize), "fluid_nodes": nf,
         "lattice_nodes": info.n_lattice_nodes, "chunks": info.n_chunks, "run_axis": info.run_axis,
-        "nodes_per_lane": info.nodes_per_lane, "warps_per_block": info.warps_per_block,
+        "nodes_per_lane": info.nodes_per_lane, "piece_slots": info.piece_slots,
+        "warps_per_block": info.warps_per_block,
         "geometry_s": t_geom, "voxelize_ms": g.info.voxelize_ms, "lattice_build_s": t_build,
         "steps": steps, "warmup": warmup, "ms_per_step": sec / steps * 1e3, "mlups": nf * steps / sec / 1e6,
         "gbs_algorithmic": info.algorithmic_bytes_per_update * nf * steps / sec / 1e9,

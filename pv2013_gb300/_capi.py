@@ -71,7 +71,7 @@ class SimParams(C.Structure):
     _fields_ = [("Q", C.c_int32), ("precision", C.c_int32), ("pattern", C.c_int32), ("tau", C.c_double),
                 ("bcs", C.POINTER(ListBC)), ("nbcs", C.c_size_t), ("warps_per_block", C.c_int32),
                 ("run_axis", C.c_int32), ("staging", C.c_int32), ("nodes_per_lane", C.c_int32),
-                ("corrections", C.c_int32)]
+                ("corrections", C.c_int32), ("piece_slots", C.c_int32)]
 
 
 class TuneEntry(C.Structure):
@@ -89,7 +89,7 @@ class SimInfo(C.Structure):
                 ("n_chunks", C.c_int64), ("Q", C.c_int32), ("precision", C.c_int32), ("pattern", C.c_int32),
                 ("warps_per_block", C.c_int32), ("run_axis", C.c_int32), ("state_bytes", C.c_int64),
                 ("algorithmic_bytes_per_update", C.c_double), ("n_lattice_nodes", C.c_int64),
-                ("nodes_per_lane", C.c_int32), ("reserved", C.c_int32)]
+                ("nodes_per_lane", C.c_int32), ("piece_slots", C.c_int32)]
 
 
 class Monitors(C.Structure):

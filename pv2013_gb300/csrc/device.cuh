@@ -156,6 +156,7 @@ struct StepArgs {
     const int32_t* out_pos;   // output position of each node (x-major rank of the fluid point)
     int64_t n_nodes;
     uint32_t corr;            // lbm_sim_params.corrections (LBM_FIX_* bits)
+    int32_t piece_lg;         // paired kernel: log2 of the lanes per chunk piece (2, 3 or 4)
 };
 
 }  // namespace lbm

@@ -279,6 +279,7 @@ struct FillArgs {
     int64_t nz;
     int64_t node_off, zslot_off, mslot_base;
     int32_t inst;
+    int32_t piece;                // node slots per paired chunk piece (k_col_fill2)
     Chunk* chunks;
     uint32_t* mmask;
     int32_t* err;
@@ -354,8 +355,9 @@ __global__ void k_col_fill(FillArgs A) {
 }
 
 // Paired chunks: each fluid run [rf, re] of a column widened to whole pairs
-// [rf & ~1, re | 1] (the added slots are ghost nodes) and cut every 32 slots.
-__global__ void k_col_count2(const uint8_t* __restrict__ type, Pad D, int32_t* __restrict__ nchunk) {
+// [rf & ~1, re | 1] (the added slots are ghost nodes) and cut every `piece`
+// slots (8, 16 or 32).
+__global__ void k_col_count2(const uint8_t* __restrict__ type, Pad D, int piece, int32_t* __restrict__ nchunk) {
     const int64_t ncol = (int64_t)D.Na * D.Nb;
     for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncol; c += (int64_t)gridDim.x * blockDim.x) {
         const int64_t a = c / D.Nb + 1, b = c % D.Nb + 1;
@@ -367,7 +369,7 @@ __global__ void k_col_count2(const uint8_t* __restrict__ type, Pad D, int32_t* _
             if (fl && rf < 0) rf = r;
             if (!fl && rf >= 0) {
                 const int64_t r0 = rf & ~int64_t(1), r1 = (r - 1) | 1;
-                nc += (int32_t)((r1 - r0 + 1 + 31) / 32);
+                nc += (int32_t)((r1 - r0 + 1 + piece - 1) / piece);
                 rf = -1;
             }
         }
@@ -390,8 +392,8 @@ __global__ void k_col_fill2(FillArgs A) {
             if (fl || rf < 0) continue;
             const int64_t re = r - 1;
             const int64_t r1 = re | 1;
-            for (int64_t r0 = rf & ~int64_t(1); r0 <= r1; r0 += 32) {
-                const int len = (int)std::min<int64_t>(32, r1 - r0 + 1);
+            for (int64_t r0 = rf & ~int64_t(1); r0 <= r1; r0 += A.piece) {
+                const int len = (int)std::min<int64_t>(A.piece, r1 - r0 + 1);
                 const int64_t lf = std::max(r0, rf), ll = std::min(r0 + len - 1, re);   // fluid levels of the piece
                 Chunk ch;
                 const int32_t n0 = A.node_of_cell[base + r0];
@@ -503,6 +505,7 @@ constexpr int kDryWarps = 4;           // warps per block of snapshot / monitor 
 struct lbm_sim {
     int dev = 0;
     int Q = 19, store = ST_F64, pattern = LBM_PULL, wpb = 4, ra = 2, staging = 0, npl = 1;
+    int piece = 16;                // node slots per paired chunk piece (8, 16 or 32)
     uint32_t corr = 0;             // LBM_FIX_* bits
     int32_t* err = nullptr;        // device flag: a bounded wait in the step kernel gave up
     int64_t N = 0, nchunks = 0, stride = 0, nz = 0;
@@ -607,7 +610,7 @@ lbm_status count_chunks(const lbm_geometry* g, int ra, cudaStream_t st, int64_t*
 }
 
 lbm_status build_instance(const lbm_geometry* g, const lbm_sim_params* p, int Q, int32_t inst, int ra, int npl,
-                          int64_t node_off, int64_t out_off, int64_t zslot_off, int64_t mslot_off, int32_t* d_err,
+                          int piece, int64_t node_off, int64_t out_off, int64_t zslot_off, int64_t mslot_off, int32_t* d_err,
                           cudaStream_t st, InstBuild& out) {
     int dims[3];
     geometry_dims(g, dims);
@@ -742,13 +745,14 @@ lbm_status build_instance(const lbm_geometry* g, const lbm_sim_params* p, int Q,
         // paired chunks share the missing masks (same boundary-node order)
         DBuf<int64_t> coff2;
         LBM_TRY(coff2.alloc(ncol, "paired chunk offsets"));
-        k_col_count2<<<blocks_for(ncol, 128), 128, 0, st>>>(type.p, D, ccount.p);
+        k_col_count2<<<blocks_for(ncol, 128), 128, 0, st>>>(type.p, D, piece, ccount.p);
         LBM_TRY(scan::exclusive_scan(ccount.p, ncol, coff2.p, &out.nchunks2, st));
         LBM_TRY(out.chunks2.alloc(out.nchunks2, "paired chunks"));
         FillArgs f2 = fa;
         f2.chunk_off = coff2.p;
         f2.chunks = out.chunks2.p;
         f2.mmask = nullptr;
+        f2.piece = piece;
         k_col_fill2<<<blocks_for(ncol, 128), 128, 0, st>>>(f2);
         LBM_CUDA(cudaGetLastError());
         LBM_CUDA(cudaStreamSynchronize(st));   // coff2 is freed on return
@@ -770,6 +774,7 @@ lbm_status sim_launch(lbm_sim* S, int mode, bool dry, void* src, void* dst, int6
     a.out_f = of; a.out_rho = orho; a.out_u = ou; a.out_pos = S->out_pos; a.n_nodes = S->NF;
     a.mmask = S->mmask;
     a.corr = S->corr;
+    a.piece_lg = S->piece == 8 ? 2 : (S->piece == 16 ? 3 : 4);
     if (!dry && S->npl == 2) {
         a.chunks = S->chunks2;
         a.nchunks = S->nchunks2;
@@ -888,6 +893,11 @@ lbm_status sim_create(const lbm_geometry* const* g, const lbm_sim_params* p, siz
     if (S->npl == 2 && S->store == ST_F64)
         return fail(LBM_ERR_ARG, "nodes_per_lane = 2 needs FP32 or 16-bit storage (FP64 runs one node per lane)");
     if (S->wpb == 0) S->wpb = S->npl == 2 ? 1 : 4;
+    if (p0.piece_slots != 0 && p0.piece_slots != 8 && p0.piece_slots != 16 && p0.piece_slots != 32)
+        return fail(LBM_ERR_ARG, "piece_slots must be 0, 8, 16 or 32 (got %d)", p0.piece_slots);
+    // 16 slots (8 lanes) per piece: on the vascular tree 90 % of the slots
+    // hold fluid nodes (83 % with 32) for 4 B of descriptors per node
+    S->piece = p0.piece_slots != 0 ? p0.piece_slots : 16;
     if (p0.corrections & ~(LBM_FIX_BB_ALL_DIRS | LBM_FIX_LIST_NODES))
         return fail(LBM_ERR_ARG, "unknown corrections bits 0x%x", (unsigned)p0.corrections);
     S->corr = (uint32_t)p0.corrections;
@@ -928,8 +938,8 @@ lbm_status sim_create(const lbm_geometry* const* g, const lbm_sim_params* p, siz
     S->inst_off.push_back(0);
     for (size_t i = 0; i < n; ++i) {
         builds.emplace_back(new InstBuild());
-        LBM_TRY(build_instance(g[i], &p[i], S->Q, (int32_t)i, S->ra, S->store == ST_F64 ? 1 : 2, node_off, out_off,
-                               (int64_t)zall.size(), nmask, S->err, st, *builds.back()));
+        LBM_TRY(build_instance(g[i], &p[i], S->Q, (int32_t)i, S->ra, S->store == ST_F64 ? 1 : 2, S->piece, node_off,
+                               out_off, (int64_t)zall.size(), nmask, S->err, st, *builds.back()));
         const InstBuild& B = *builds.back();
         node_off += B.N;
         out_off += B.NF;
@@ -1310,7 +1320,7 @@ lbm_status lbm_sim_info_get(const lbm_sim* S, lbm_sim_info* info) {
     info->n_chunks = S->npl == 2 ? S->nchunks2 : S->nchunks;
     info->n_lattice_nodes = S->N;
     info->nodes_per_lane = S->npl;
-    info->reserved = 0;
+    info->piece_slots = S->npl == 2 ? S->piece : 0;
     info->Q = S->Q;
     info->precision = S->store;
     info->pattern = S->pattern;

@@ -1,20 +1,24 @@
-// Paired step kernel: two adjacent nodes per lane, half a warp per chunk.
+// Paired step kernel: two adjacent nodes per lane, 4, 8 or 16 lanes per chunk
+// piece.
 //
 // Same operations and streaming patterns as k_step (step_kernel.cuh), for the
 // FP32 and 16-bit storages; what changes is how a lane covers its nodes:
-//   * lane t of a half-warp owns the nodes at levels r0+2t and r0+2t+1 of its
-//     chunk (a pair).  The lattice numbers every node so that its id has the
-//     parity of its level (sim.cu), so a pair is one aligned 32-bit (16-bit
-//     storage) or 64-bit (FP32 storage) word in each population plane;
+//   * lane t of a piece's lane group owns the nodes at levels r0+2t and
+//     r0+2t+1 of its chunk (a pair).  The lattice numbers every node so that
+//     its id has the parity of its level (sim.cu), so a pair is one aligned
+//     32-bit (16-bit storage) or 64-bit (FP32 storage) word in each
+//     population plane;
 //   * a neighbour pair one level up or down straddles two aligned words: the
 //     lane loads both and takes the high half of one and the low half of the
 //     other (a byte permute, no shuffle);
 //   * the collision runs on packed FP32 pairs (add/sub/mul/fma.rn.f32x2), one
 //     instruction for both nodes;
 //   * boundary fix-ups and Zou-He run per node, only in warps that have them.
-// Chunk pieces start at even levels and hold up to 32 node slots; a slot at
-// either end may be a ghost node (not in the piece's vmask): its values are
-// computed and discarded, and in the AA odd pattern it stores nothing.
+// Chunk pieces start at even levels and hold up to 8, 16 or 32 node slots
+// (lbm_sim_params.piece_slots: shorter pieces leave fewer idle lanes where a
+// run ends, for 64 descriptor bytes per piece); a slot at either end may be a
+// ghost node (not in the piece's vmask): its values are computed and
+// discarded, and in the AA odd pattern it stores nothing.
 #pragma once
 #include "step.h"
 #include "step_kernel.cuh"
@@ -65,12 +69,12 @@ template <> struct PairWord<ST_BF16S> { using W = uint32_t; };
 
 template <int S> constexpr int elem_bytes() { return S == ST_F32 ? 4 : 2; }
 
-// the pair word holding elements off and off+1 (off even: a population
-// plane's offset plus an even node id) -- one base pointer and 32-bit element
-// offsets keep the address arithmetic in 32-bit registers
+// pair word wo of the population array: elements 2 wo and 2 wo + 1.  Plane
+// strides and pair ids are even, so word offsets (plane * stride/2 + id/2)
+// are formed directly in 32-bit registers from one base pointer
 template <int S>
-__device__ __forceinline__ typename PairWord<S>::W ldw(const void* base, uint32_t off) {
-    return reinterpret_cast<const typename PairWord<S>::W*>(base)[off >> 1];
+__device__ __forceinline__ typename PairWord<S>::W ldw(const void* base, uint32_t wo) {
+    return reinterpret_cast<const typename PairWord<S>::W*>(base)[wo];
 }
 // high element of word a, low element of word b (a pair one level out of phase)
 template <int S>
@@ -109,8 +113,8 @@ __device__ __forceinline__ typename PairWord<S>::W pack(F2 v, int q) {
     }
 }
 template <int S>
-__device__ __forceinline__ void stw(void* base, uint32_t off, typename PairWord<S>::W w) {
-    reinterpret_cast<typename PairWord<S>::W*>(base)[off >> 1] = w;
+__device__ __forceinline__ void stw(void* base, uint32_t wo, typename PairWord<S>::W w) {
+    reinterpret_cast<typename PairWord<S>::W*>(base)[wo] = w;
 }
 // one element (one node) of a plane
 template <int S, int Q>
@@ -271,8 +275,11 @@ __global__ void __launch_bounds__(256) __maxnreg__((PairMaxReg<Q, S, MODE>::valu
     using X = Ax<Q, RA>;
     using W = typename PairWord<S>::W;
     const int lane = threadIdx.x & 31;
-    const int t = lane & 15;                      // pair index within the chunk
-    const int64_t ci = ((int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 2 + (lane >> 4);
+    // a chunk piece is served by 2^lg lanes (4, 8 or 16): 32 >> lg pieces per warp
+    const int lg = a.piece_lg;
+    const int t = lane & ((1 << lg) - 1);         // pair index within the chunk
+    const int pw = lane >> lg;                    // piece of this lane within the warp
+    const int64_t ci = (((int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) << (5 - lg)) + pw;
     const bool have_chunk = ci < a.nchunks;
     // chunk descriptor words 0-7 (n0, len_inst, wmask, zmask, bmask, zslot0, mslot0, K0)
     const uint4* cw = reinterpret_cast<const uint4*>(a.chunks + (have_chunk ? ci : 0));
@@ -292,6 +299,7 @@ __global__ void __launch_bounds__(256) __maxnreg__((PairMaxReg<Q, S, MODE>::valu
     }
     const uint32_t e = (uint32_t)(n0 + 2 * t);     // id of the lo node (even)
     const uint32_t st = (uint32_t)a.stride;
+    const uint32_t sw = st >> 1, ew = (uint32_t)(n0 >> 1) + (uint32_t)t;   // word offsets: plane stride, the pair's word
     const int64_t step = a.step + (a.step_base ? *a.step_base : 0);
     const void* A = a.src;
 
@@ -315,27 +323,28 @@ __global__ void __launch_bounds__(256) __maxnreg__((PairMaxReg<Q, S, MODE>::valu
     };
 
     W raw[Q];
-    __shared__ int32_t ksm[8][2][8];     // column bases of each warp's two chunks
+    __shared__ int32_t ksm[8][8][8];     // column bases of each warp's chunks
     if (act) {
         int32_t K[8];
         if constexpr (MODE != MODE_AA_EVEN) load_K(K, false);
         if constexpr (MODE == MODE_AA_ODD) {
             if (t == 0) {
 #pragma unroll
-                for (int c = 0; c < 8; ++c) ksm[threadIdx.x >> 5][lane >> 4][c] = K[c];
+                for (int c = 0; c < 8; ++c) ksm[threadIdx.x >> 5][pw][c] = K[c];
             }
         }
 #pragma unroll
         for (int q = 0; q < Q; ++q) {
             if constexpr (MODE == MODE_AA_EVEN) {
-                raw[q] = ldw<S>(A, (uint32_t)q * st + e);
+                raw[q] = ldw<S>(A, (uint32_t)q * sw + ew);
             } else {
                 const int da = -X::a(q), db = -X::b(q), o = -X::r(q);
-                const uint32_t pb = (uint32_t)(MODE == MODE_AA_ODD ? L::opp(q) : q) * st;
-                const uint32_t s = (uint32_t)((da == 0 && db == 0 ? n0 - 1 : K[col8(da, db)]) + 1 + 2 * t);
+                // word of the neighbour column's pair at the same levels (K + 1 is even)
+                const uint32_t pb = (uint32_t)(MODE == MODE_AA_ODD ? L::opp(q) : q) * sw;
+                const uint32_t s = (da == 0 && db == 0) ? ew : ((uint32_t)(K[col8(da, db)] + 1) >> 1) + (uint32_t)t;
                 if (o == 0) raw[q] = ldw<S>(A, pb + s);
-                else if (o > 0) raw[q] = straddle<S>(ldw<S>(A, pb + s), ldw<S>(A, pb + s + 2));
-                else raw[q] = straddle<S>(ldw<S>(A, pb + s - 2), ldw<S>(A, pb + s));
+                else if (o > 0) raw[q] = straddle<S>(ldw<S>(A, pb + s), ldw<S>(A, pb + s + 1));
+                else raw[q] = straddle<S>(ldw<S>(A, pb + s - 1), ldw<S>(A, pb + s));
             }
         }
     }
@@ -361,7 +370,7 @@ __global__ void __launch_bounds__(256) __maxnreg__((PairMaxReg<Q, S, MODE>::valu
                     // bounce-back source: own node, slot opp(q) (pull) or slot q (AA
                     // odd); a predicated load and selects instead of branches
                     W own = raw[q];
-                    if (bl || bh) own = ldw<S>(A, (uint32_t)(MODE == MODE_PULL ? L::opp(q) : q) * st + e);
+                    if (bl || bh) own = ldw<S>(A, (uint32_t)(MODE == MODE_PULL ? L::opp(q) : q) * sw + ew);
                     raw[q] = take_half<S>(raw[q], false, bl ? own : raw[q]);
                     raw[q] = take_half<S>(raw[q], true, bh ? own : raw[q]);
                 }
@@ -393,23 +402,23 @@ __global__ void __launch_bounds__(256) __maxnreg__((PairMaxReg<Q, S, MODE>::valu
     const float om = a.insts[li >> 8].omega_f;
     void* D = a.dst;
     if constexpr (MODE == MODE_PULL) {
-        collide2<Q, S>(raw, om, [&](int q, F2 v) { stw<S>(D, (uint32_t)q * st + e, pack<S, Q>(v, q)); });
+        collide2<Q, S>(raw, om, [&](int q, F2 v) { stw<S>(D, (uint32_t)q * sw + ew, pack<S, Q>(v, q)); });
     } else if constexpr (MODE == MODE_AA_EVEN) {
-        collide2<Q, S>(raw, om, [&](int q, F2 v) { stw<S>(D, (uint32_t)L::opp(q) * st + e, pack<S, Q>(v, q)); });
+        collide2<Q, S>(raw, om, [&](int q, F2 v) { stw<S>(D, (uint32_t)L::opp(q) * sw + ew, pack<S, Q>(v, q)); });
     } else {
         // AA odd: f*_q to slot q of x + c_q, or (absent destination) to slot
         // opp(q) of x; ghost slots of the pair store nothing
         uint32_t vm;
         asm volatile("ld.global.nc.u32 %0, [%1];" : "=r"(vm) : "l"(&cw[3].w));
         vm = (vm >> (2 * t)) & 3u;
-        const volatile int32_t* ks = ksm[threadIdx.x >> 5][lane >> 4];
+        const volatile int32_t* ks = ksm[threadIdx.x >> 5][pw];
         collide2<Q, S>(raw, om, [&](int q, F2 v) {
             const int da = X::a(q), db = X::b(q), o = X::r(q);
             const uint32_t s = (uint32_t)((da == 0 && db == 0 ? n0 - 1 : ks[col8(da, db)]) + 1 + 2 * t);
             const bool bl = (m_lo >> L::opp(q)) & 1u, bh = (m_hi >> L::opp(q)) & 1u;
             const uint32_t pq = (uint32_t)q * st, po = (uint32_t)L::opp(q) * st;
             if (o == 0 && vm == 3u && !bl && !bh) {
-                stw<S>(D, pq + s, pack<S, Q>(v, q));
+                stw<S>(D, (uint32_t)q * sw + (s >> 1), pack<S, Q>(v, q));
             } else {
                 float l, h;
                 f2split(v, l, h);
@@ -421,7 +430,7 @@ __global__ void __launch_bounds__(256) __maxnreg__((PairMaxReg<Q, S, MODE>::valu
 }
 
 // ---------------------------------------------------------------------------
-// launch: two chunks per warp, wpb warps per block
+// launch: 32 / 2^piece_lg chunk pieces per warp, wpb warps per block
 template <int Q, int S, int MODE, int RA>
 static lbm_status launch_pair_one(const StepArgs& a, int wpb, cudaStream_t st) {
     // dynamic shared memory: one word per population and lane of each warp
@@ -434,7 +443,7 @@ static lbm_status launch_pair_one(const StepArgs& a, int wpb, cudaStream_t st) {
         if (e != cudaSuccess) return fail(LBM_ERR_CUDA, "paired step kernel shared memory: %s", cudaGetErrorString(e));
         opted = (int)smem;
     }
-    const int64_t per_block = 2 * (int64_t)wpb;
+    const int64_t per_block = (int64_t)wpb << (5 - a.piece_lg);
     const int64_t blocks = (a.nchunks + per_block - 1) / per_block;
     k_step2<Q, S, MODE, RA><<<(unsigned)(blocks > 0 ? blocks : 1), 32 * wpb, smem, st>>>(a);
     return LBM_OK;

@@ -264,7 +264,7 @@ PATTERNS = {"pull": _capi.PULL, "aa": _capi.AA, "auto": _capi.AUTO}
 
 
 def _params(Q, precision, pattern, tau, bcs, warps_per_block, run_axis=0, staging=0, nodes_per_lane=0,
-            corrections=0):
+            corrections=0, piece_slots=0):
     cb = [b.to_c() for b in bcs]
     arr = (_capi.ListBC * max(len(cb), 1))(*cb)
     p = _capi.SimParams()
@@ -279,6 +279,7 @@ def _params(Q, precision, pattern, tau, bcs, warps_per_block, run_axis=0, stagin
     p.staging = int(staging)
     p.nodes_per_lane = int(nodes_per_lane)
     p.corrections = int(corrections)
+    p.piece_slots = int(piece_slots)
     return p, arr
 
 
@@ -290,7 +291,7 @@ class Simulation:
     """
 
     def __init__(self, geometry, tau, bcs=(), Q=19, precision="f64", pattern="pull", warps_per_block=0, run_axis=0,
-                 staging=0, stream=None, nodes_per_lane=0, corrections=0):
+                 staging=0, stream=None, nodes_per_lane=0, corrections=0, piece_slots=0):
         lib = load()
         self._stream = C.c_void_p(stream) if stream else None
         h = C.c_void_p()
@@ -302,7 +303,7 @@ class Simulation:
             params = (_capi.SimParams * n)()
             for i in range(n):
                 p, arr = _params(Q, precision, pattern, taus[i], bcl[i], warps_per_block, run_axis, staging, nodes_per_lane,
-                                 corrections)
+                                 corrections, piece_slots)
                 keep.append((arr, bcl[i]))
                 params[i] = p
             geoms = (C.c_void_p * n)(*[g.handle for g in geometry])
@@ -310,7 +311,7 @@ class Simulation:
             self.geometries = list(geometry)
         else:
             p, arr = _params(Q, precision, pattern, tau, bcs, warps_per_block, run_axis, staging, nodes_per_lane,
-                             corrections)
+                             corrections, piece_slots)
             check(lib.lbm_sim_create(geometry.handle, C.byref(p), self._stream, C.byref(h)))
             self.geometries = [geometry]
         self._h = h

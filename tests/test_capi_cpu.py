@@ -34,7 +34,7 @@ def test_library_exports_every_declared_symbol():
     for n in sorted(names):
         assert hasattr(lib, n), n
     assert set(_capi.PROTOTYPES) == names
-    assert lib.lbm_abi_version() == 2
+    assert lib.lbm_abi_version() == 3
 
 
 def test_status_strings():

@@ -152,3 +152,45 @@ def test_autotune_keeps_state_and_results(pattern):
     a.step(40, graph=True)
     b.step(40, graph=True)
     assert rel_l2(b.fields()[0], a.fields()[0]) < 1e-6
+
+
+@pytest.mark.parametrize("precision,pattern", [("f16s", "aa"), ("f32", "pull"), ("bf16s", "aa")])
+def test_piece_sizes_give_identical_results(precision, pattern):
+    """The chunk piece size changes which lanes serve which nodes, not the
+    per-node arithmetic: 8-, 16- and 32-slot pieces give the same bits, on a
+    pulsatile vessel (walls, inlet and outlet nodes at piece ends) and on a
+    two-member batch."""
+    c = cases.vessel(4004)
+    geom = c.geometry()
+    out = {}
+    for piece in (8, 16, 32):
+        sim = Simulation(geom, c.tau, c.boundary_specs(geom), precision=precision, pattern=pattern,
+                         nodes_per_lane=2, piece_slots=piece)
+        info = sim.info()
+        assert info.piece_slots == piece and info.nodes_per_lane == 2
+        sim.step(57, graph=True)
+        out[piece] = sim.fields()[0]
+    assert np.isfinite(out[16]).all()
+    assert np.array_equal(out[8], out[16]) and np.array_equal(out[32], out[16])
+    # chunk counts: shorter pieces, more chunks
+    c1, c2 = cases.pipe(), cases.vessel(4005)
+    g1, g2 = c1.geometry(), c2.geometry()
+    runs = {}
+    for piece in (8, 32):
+        b = Simulation([g1, g2], [c1.tau, c2.tau], [c1.boundary_specs(g1), c2.boundary_specs(g2)],
+                       precision=precision, pattern=pattern, piece_slots=piece)
+        runs[piece] = (b.info().n_chunks, b)
+        b.step(31, graph=True)
+    assert runs[8][0] > runs[32][0]
+    assert np.array_equal(runs[8][1].fields()[0], runs[32][1].fields()[0])
+
+
+def test_piece_size_default_and_arguments():
+    c = cases.pipe()
+    geom = c.geometry()
+    assert Simulation(geom, c.tau, c.boundary_specs(geom), precision="f16s", pattern="aa").info().piece_slots == 16
+    assert Simulation(geom, c.tau, c.boundary_specs(geom), precision="f64").info().piece_slots == 0
+    for bad in (4, 12, 64, -1):
+        with pytest.raises(_capi.LbmError) as e:
+            Simulation(geom, c.tau, c.boundary_specs(geom), precision="f16s", pattern="aa", piece_slots=bad)
+        assert e.value.status == _capi.ERR_ARG
