@@ -75,6 +75,20 @@ typedef struct lbm_tri {
  * vertex/endloop/endfacet lines parse in sequence) and correctly rounded
  * decimal conversion.  *tris is allocated by the library (lbm_free).       */
 lbm_status lbm_stl_read_ascii(const char* path, lbm_tri** tris, size_t* n);
+
+/* The same reader with the parsing on the GPU (no counterpart in the
+ * reference, whose reader is GeometryReader.cpp:33-117): the file is copied
+ * to the device, facets are located and checked line by line in parallel,
+ * and the numbers are converted with exact integer arithmetic (bit-identical
+ * to the host reader's correctly rounded conversion).  Files outside the
+ * canonical facet layout, or holding a number outside the exact converter's
+ * scope (more than 19 significant digits, |decimal exponent| > 27), are
+ * parsed by the host grammar instead; *on_device (may be NULL) is 1 when the
+ * GPU produced the result.  The result equals lbm_stl_read_ascii's in every
+ * case.  Work runs on `stream` (a cudaStream_t, NULL = default stream);
+ * LBM_ERR_NODEV without a CUDA device. */
+lbm_status lbm_stl_read_ascii_device(const char* path, void* stream, lbm_tri** tris, size_t* n,
+                                     int32_t* on_device);
 /* Binary STL reader; replaces Reader::readSTLBinary (GeometryReader.cpp:
  * 119-176): float vertices widened to double, normals renormalised in float. */
 lbm_status lbm_stl_read_binary(const char* path, lbm_tri** tris, size_t* n);

@@ -106,6 +106,7 @@ PROTOTYPES = {
     "lbm_abi_version": (C.c_int, []),
     "lbm_stl_read_ascii": (C.c_int, [C.c_char_p, _P(_P(Tri)), _P(C.c_size_t)]),
     "lbm_stl_read_binary": (C.c_int, [C.c_char_p, _P(_P(Tri)), _P(C.c_size_t)]),
+    "lbm_stl_read_ascii_device": (C.c_int, [C.c_char_p, C.c_void_p, _P(_P(Tri)), _P(C.c_size_t), _P(C.c_int32)]),
     "lbm_stl_write_ascii": (C.c_int, [C.c_char_p, _P(Tri), C.c_size_t, C.c_char_p]),
     "lbm_geometry_create": (C.c_int, [_P(Tri), C.c_size_t, C.c_double, _P(Grid), _P(Predicate), C.c_size_t,
                                       C.c_void_p, _P(C.c_void_p)]),

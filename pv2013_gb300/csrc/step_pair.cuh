@@ -284,6 +284,12 @@ __global__ void __launch_bounds__(256) __maxnreg__((PairMaxReg<Q, S, MODE>::valu
     // chunk descriptor words 0-7 (n0, len_inst, wmask, zmask, bmask, zslot0, mslot0, K0)
     const uint4* cw = reinterpret_cast<const uint4*>(a.chunks + (have_chunk ? ci : 0));
     const uint4 d0 = have_chunk ? __ldg(cw) : make_uint4(0u, 0u, 0u, 0u);
+    // start id of the piece one wave of resident warps ahead: its population
+    // windows are prefetched into L2 below (the load is in flight with d0)
+    const int64_t cfp = ci + a.pf_ahead;
+    const bool hfp = a.pf_ahead > 0 && cfp < a.nchunks;
+    uint32_t nfp = 0;
+    if (hfp) asm volatile("ld.global.nc.u32 %0, [%1];" : "=r"(nfp) : "l"(&a.chunks[cfp].n0));
     const uint4 d1 = have_chunk ? __ldg(cw + 1) : make_uint4(0u, 0u, 0u, 0u);
     const int32_t n0 = (int32_t)d0.x;
     const uint32_t li = d0.y;
@@ -349,6 +355,21 @@ __global__ void __launch_bounds__(256) __maxnreg__((PairMaxReg<Q, S, MODE>::valu
         }
     }
 
+    // L2 prefetch of that piece's window in every plane: lane t of the piece's
+    // lane group takes planes t, t + 2^lg, ... (words n0/2 - 1 and n0/2 + 2^lg,
+    // the ends of the window with its straddle words).  Neighbour columns'
+    // windows are the windows of nearby pieces, prefetched by them.  Ids
+    // stay in [8, N - 8), so both words lie inside the population array.
+    if (hfp) {
+        const uint32_t wf = nfp >> 1, wl = wf + (1u << lg);
+        const char* Ab = reinterpret_cast<const char*>(A);
+        for (int q = t; q < Q; q += 1 << lg) {
+            const char* p0 = Ab + (size_t)((uint32_t)q * sw + wf - 1u) * sizeof(W);
+            const char* p1 = Ab + (size_t)((uint32_t)q * sw + wl) * sizeof(W);
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(p0));
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(p1));
+        }
+    }
     // the odd pattern's column bases go through shared memory (lane 0 of
     // each chunk wrote them): fewer registers held across the collision
     if constexpr (MODE == MODE_AA_ODD) __syncwarp();
@@ -445,7 +466,19 @@ static lbm_status launch_pair_one(const StepArgs& a, int wpb, cudaStream_t st) {
     }
     const int64_t per_block = (int64_t)wpb << (5 - a.piece_lg);
     const int64_t blocks = (a.nchunks + per_block - 1) / per_block;
-    k_step2<Q, S, MODE, RA><<<(unsigned)(blocks > 0 ? blocks : 1), 32 * wpb, smem, st>>>(a);
+    // prefetch distance: the pieces of one wave of resident blocks
+    static int resident[9] = {0};
+    if (resident[wpb] == 0) {
+        int dev = 0, sms = 0, nb = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_step2<Q, S, MODE, RA>, 32 * wpb, smem) != cudaSuccess)
+            return fail(LBM_ERR_CUDA, "paired step kernel occupancy: %s", cudaGetErrorString(cudaGetLastError()));
+        resident[wpb] = sms * (nb > 0 ? nb : 1);
+    }
+    StepArgs b = a;
+    b.pf_ahead = (int64_t)resident[wpb] * per_block;
+    k_step2<Q, S, MODE, RA><<<(unsigned)(blocks > 0 ? blocks : 1), 32 * wpb, smem, st>>>(b);
     return LBM_OK;
 }
 

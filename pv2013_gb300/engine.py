@@ -46,6 +46,19 @@ class Reader:
         return _tri_array(p, n.value)
 
     @staticmethod
+    def readSTLASCIIDevice(path, stream=None):
+        """readSTLASCII with the parsing on the GPU; returns (triangles,
+        on_device) -- on_device False when the file needed the host grammar
+        (the triangles are the same either way)."""
+        lib = load()
+        p = C.POINTER(_capi.Tri)()
+        n = C.c_size_t()
+        on = C.c_int32()
+        check(lib.lbm_stl_read_ascii_device(str(path).encode(), C.c_void_p(stream) if stream else None, C.byref(p),
+                                            C.byref(n), C.byref(on)))
+        return _tri_array(p, n.value), bool(on.value)
+
+    @staticmethod
     def readSTLBinary(path):
         lib = load()
         p = C.POINTER(_capi.Tri)()

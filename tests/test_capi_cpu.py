@@ -159,3 +159,14 @@ def test_geometry_without_device_fails_cleanly():
     with pytest.raises(_capi.LbmError) as e:
         c.geometry()
     assert e.value.status == 9
+
+
+def test_device_stl_reader_without_device_fails_cleanly(tmp_path):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a device is present")
+    p = tmp_path / "t.stl"
+    Reader.writeSTLASCII(p, cases.pipe().triangles[:3])
+    with pytest.raises(_capi.LbmError) as e:
+        Reader.readSTLASCIIDevice(p)
+    assert e.value.status == 9
