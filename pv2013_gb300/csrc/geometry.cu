@@ -68,13 +68,23 @@ __device__ __forceinline__ void column_xy(const VoxGrid& g, int i, int j, double
     if (sy == g.bb[3]) sy -= off;
 }
 
-// Enumerates candidate columns of triangle T and calls fn(col) for those
-// passing the exact xy test.  Returns false when the projection is degenerate
-// to a point (such a triangle is tested by every column instead).
+// Candidate columns of triangle T, in two parts.  enum_box calls fn(col) for
+// the columns of the projection's bounding box that pass the exact xy test
+// and returns kPointLike when the projection is degenerate to a point (such
+// a triangle is tested by every column instead), kNeedle when it is so thin
+// that the xy test can also pass on its supporting line outside the box, and
+// kBoxOnly otherwise.  enum_band covers the needle case: a band around the
+// supporting line of the longest edge across the whole grid, the columns
+// lane, lane + nl, ... of it (a warp shares one triangle's band).
+constexpr int kPointLike = 0, kBoxOnly = 1, kNeedle = 2;
+
+struct BoxRange {
+    long i0, i1, j0, j1;
+};
+
 template <class F>
-__device__ bool enumerate_columns(const VoxGrid& g, const double* T, F fn) {
+__device__ int enum_box(const VoxGrid& g, const double* T, BoxRange& r, F fn) {
     const double s = g.spacing;
-    const int pad = 2 + (int)ceil(0.01 / s);
     const double xmn = fmin(T[0], fmin(T[3], T[6])), xmx = fmax(T[0], fmax(T[3], T[6]));
     const double ymn = fmin(T[1], fmin(T[4], T[7])), ymx = fmax(T[1], fmax(T[4], T[7]));
     // columns whose ray (min + i*s, nudged by at most 0.01 at the grid faces)
@@ -91,8 +101,34 @@ __device__ bool enumerate_columns(const VoxGrid& g, const double* T, F fn) {
         while (i >= 0 && base + (double)i * s > v) --i;
         return i;
     };
-    const long i0 = lower(xmn - 0.01, g.bb[0], g.Nx), i1 = upper(xmx + 0.01, g.bb[0], g.Nx);
-    const long j0 = lower(ymn - 0.01, g.bb[2], g.Ny), j1 = upper(ymx + 0.01, g.bb[2], g.Ny);
+    r.i0 = lower(xmn - 0.01, g.bb[0], g.Nx);
+    r.i1 = upper(xmx + 0.01, g.bb[0], g.Nx);
+    r.j0 = lower(ymn - 0.01, g.bb[2], g.Ny);
+    r.j1 = upper(ymx + 0.01, g.bb[2], g.Ny);
+    double ex[3] = {T[3] - T[0], T[6] - T[3], T[0] - T[6]};
+    double ey[3] = {T[4] - T[1], T[7] - T[4], T[1] - T[7]};
+    double best = -1.0;
+    for (int m = 0; m < 3; ++m) {
+        double l = fabs(ex[m]) + fabs(ey[m]);
+        if (l > best) best = l;
+    }
+    const double scale = 1.0 + fmax(fmax(fabs(xmn), fabs(xmx)), fmax(fabs(ymn), fabs(ymx)));
+    if (!(best > 1e-9 * scale)) return kPointLike;    // point-like projection: every column tests it
+    for (long i = r.i0; i <= r.i1; ++i)
+        for (long j = r.j0; j <= r.j1; ++j) {
+            double sx, sy;
+            column_xy(g, (int)i, (int)j, sx, sy);
+            if (inside2d(sx, sy, T)) fn(i * (long)g.Ny + j);
+        }
+    // needle-thin projection: the band below is needed as well
+    const double area2 = fabs((T[3] - T[0]) * (T[7] - T[1]) - (T[4] - T[1]) * (T[6] - T[0]));
+    return area2 > 1e-9 * best * scale ? kBoxOnly : kNeedle;   // height above 1e-9 relative: box is enough
+}
+
+template <class F>
+__device__ void enum_band(const VoxGrid& g, const double* T, const BoxRange& r, int lane, int nl, F fn) {
+    const double s = g.spacing;
+    const int bp = 2 + (int)ceil(0.01 / s);
     double ex[3] = {T[3] - T[0], T[6] - T[3], T[0] - T[6]};
     double ey[3] = {T[4] - T[1], T[7] - T[4], T[1] - T[7]};
     int e = 0;
@@ -101,24 +137,11 @@ __device__ bool enumerate_columns(const VoxGrid& g, const double* T, F fn) {
         double l = fabs(ex[m]) + fabs(ey[m]);
         if (l > best) { best = l; e = m; }
     }
-    const double scale = 1.0 + fmax(fmax(fabs(xmn), fabs(xmx)), fmax(fabs(ymn), fabs(ymx)));
-    if (!(best > 1e-9 * scale)) return false;    // point-like projection: every column tests it
-    for (long i = i0; i <= i1; ++i)
-        for (long j = j0; j <= j1; ++j) {
-            double sx, sy;
-            column_xy(g, (int)i, (int)j, sx, sy);
-            if (inside2d(sx, sy, T)) fn(i * (long)g.Ny + j);
-        }
-    // needle-thin projection: also scan a band around the supporting line of
-    // the longest edge across the whole grid
-    const double area2 = fabs((T[3] - T[0]) * (T[7] - T[1]) - (T[4] - T[1]) * (T[6] - T[0]));
-    if (area2 > 1e-9 * best * scale) return true;  // height above 1e-9 relative: box is enough
     const double ox = T[3 * e], oy = T[3 * e + 1];
     const double dx = ex[e], dy = ey[e];
-    const int bp = pad;
     if (fabs(dx) >= fabs(dy)) {
-        for (long i = 0; i < g.Nx; ++i) {
-            if (i >= i0 && i <= i1) continue;
+        for (long i = lane; i < g.Nx; i += nl) {
+            if (i >= r.i0 && i <= r.i1) continue;
             double sx, sy;
             column_xy(g, (int)i, 0, sx, sy);
             double y = oy + (sx - ox) * (dy / dx);
@@ -129,8 +152,8 @@ __device__ bool enumerate_columns(const VoxGrid& g, const double* T, F fn) {
             }
         }
     } else {
-        for (long j = 0; j < g.Ny; ++j) {
-            if (j >= j0 && j <= j1) continue;
+        for (long j = lane; j < g.Ny; j += nl) {
+            if (j >= r.j0 && j <= r.j1) continue;
             double sx, sy;
             column_xy(g, 0, (int)j, sx, sy);
             double x = ox + (sy - oy) * (dx / dy);
@@ -141,30 +164,55 @@ __device__ bool enumerate_columns(const VoxGrid& g, const double* T, F fn) {
             }
         }
     }
-    return true;
+}
+
+// One thread per triangle for the box; the warp's needle triangles then
+// take turns, each band scanned by all 32 lanes.  Threads past the end
+// stay for the warp-wide vote.
+template <class FMake>
+__device__ void enumerate_warp(const VoxGrid& g, const double* tris, int64_t t, int64_t ntris, FMake make_fn,
+                               int32_t* global_list, int32_t* nglobal) {
+    const int lane = threadIdx.x & 31;
+    const bool valid = t < ntris;
+    int kind = kBoxOnly;
+    BoxRange r = {0, -1, 0, -1};
+    if (valid) {
+        kind = enum_box(g, tris + 12 * t, r, make_fn(t));
+        if (kind == kPointLike && global_list) {
+            const int slot = atomicAdd(nglobal, 1);
+            global_list[slot] = (int32_t)t;
+        }
+    }
+    unsigned m = __ballot_sync(0xffffffffu, valid && kind == kNeedle);
+    while (m) {
+        const int src = __ffs(m) - 1;
+        m &= m - 1;
+        const long long ts = __shfl_sync(0xffffffffu, (long long)t, src);
+        BoxRange rs;
+        rs.i0 = __shfl_sync(0xffffffffu, (long long)r.i0, src);
+        rs.i1 = __shfl_sync(0xffffffffu, (long long)r.i1, src);
+        rs.j0 = __shfl_sync(0xffffffffu, (long long)r.j0, src);
+        rs.j1 = __shfl_sync(0xffffffffu, (long long)r.j1, src);
+        enum_band(g, tris + 12 * ts, rs, lane, 32, make_fn((int64_t)ts));
+    }
 }
 
 __global__ void k_tri_count(VoxGrid g, const double* __restrict__ tris, int64_t ntris, int32_t* __restrict__ colcount,
                             int32_t* __restrict__ global_list, int32_t* __restrict__ nglobal) {
-    int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (t >= ntris) return;
-    const double* T = tris + 12 * t;
-    bool ok = enumerate_columns(g, T, [&](long col) { atomicAdd(&colcount[col], 1); });
-    if (!ok) {
-        int slot = atomicAdd(nglobal, 1);
-        global_list[slot] = (int32_t)t;
-    }
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    enumerate_warp(g, tris, t, ntris, [&](int64_t) { return [colcount](long col) { atomicAdd(&colcount[col], 1); }; },
+                   global_list, nglobal);
 }
 
 __global__ void k_tri_fill(VoxGrid g, const double* __restrict__ tris, int64_t ntris, const int64_t* __restrict__ colstart,
                            int32_t* __restrict__ cursor, int32_t* __restrict__ pairs) {
-    int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (t >= ntris) return;
-    const double* T = tris + 12 * t;
-    enumerate_columns(g, T, [&](long col) {
-        int slot = atomicAdd(&cursor[col], 1);
-        pairs[colstart[col] + slot] = (int32_t)t;
-    });
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    enumerate_warp(g, tris, t, ntris, [&](int64_t tt) {
+        return [=](long col) {
+            int slot = atomicAdd(&cursor[col], 1);
+            pairs[colstart[col] + slot] = (int32_t)tt;
+        };
+    }, nullptr, nullptr);
 }
 
 // Per-candidate plane terms staged in shared memory.
