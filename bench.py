@@ -149,7 +149,7 @@ def reference_sample(case):
     return sub, (float(x0), float(y0), float(z0)), (96, y1 - y0, 96)
 
 
-def run_reference_sample(case, sample, steps, workdir, tag):
+def run_reference_sample(case, sample, steps, workdir, tag, warmup=0):
     """One reference process on the sample; returns (fluid nodes, steps, seconds)."""
     from oracle import oracle as O
     sub, origin, dims = sample
@@ -165,7 +165,8 @@ def run_reference_sample(case, sample, steps, workdir, tag):
     pred = [(0, (1, repr(float(plane)), 1e-2, (case.inlet.center[0] - 44, math.nan, case.inlet.center[1] - 44),
                  (case.inlet.center[0] + 44, math.nan, case.inlet.center[1] + 44)))]
     res = O.run_reference(stl, 1.0, grid=(origin, dims), preds=pred, tau=case.tau, outlet_rho=1.0, steps=steps,
-                          profile=None, amp=None, workdir=os.path.join(workdir, tag), flags_path=fpath)
+                          profile=None, amp=None, workdir=os.path.join(workdir, tag), flags_path=fpath,
+                          warmup=warmup)
     t = res["time"]
     return t["nodes"], t["steps"], t["seconds"]
 
@@ -192,15 +193,16 @@ def reference_arm(args):
         os.makedirs(os.path.join(wd, f"p{d}"), exist_ok=True)
     t0 = time.time()
     with ThreadPoolExecutor(max_workers=cores) as ex:
-        res = list(ex.map(lambda d: run_reference_sample(case, sample, steps, wd, f"p{d}"), range(cores)))
+        res = list(ex.map(lambda d: run_reference_sample(case, sample, steps, wd, f"p{d}", args.warmup), range(cores)))
     wall = time.time() - t0
     mlups = sum(n * s / sec for n, s, sec in res) / 1e6
     nodes = res[0][0]
     return {"metric": METRIC, "value": mlups, "unit": "MLUPS", "impl": "reference", "n_gpus": 0,
-            "steps": steps, "warmup": 0, "higher_is_better": True, "dtype": "f64", "data": "synthetic",
+            "steps": steps, "warmup": args.warmup, "higher_is_better": True, "dtype": "f64", "data": "synthetic",
             "config": {"workload": WORKLOAD, "sample": "inlet section 96x40x96 points", "processes": cores},
             "cpu_baseline": {"value": mlups, "unit": "MLUPS", "cores": cores, "kind": "reference",
-                             "sample": f"{cores} concurrent reference processes, each {steps} steps on the "
+                             "sample": f"{cores} concurrent reference processes, each {args.warmup} untimed + "
+                                       f"{steps} timed steps on the "
                                        f"{nodes}-node inlet section of the tree (reference voxelizer bypassed: "
                                        f"flags from the oracle); step-loop seconds only; wall {wall:.1f}s"},
             "e2e": {"value": mlups, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -320,7 +322,7 @@ def gpu_arm(args, rank, world):
             if not O.ref_available(19):
                 O.build()
             wd = tempfile.mkdtemp(prefix="pv2013_cpu_")
-            n, s, sec = run_reference_sample(case, reference_sample(case), 30, wd, "p0")
+            n, s, sec = run_reference_sample(case, reference_sample(case), 30, wd, "p0", warmup=3)
             cpu = {"value": n * s / sec / 1e6, "unit": "MLUPS", "cores": 1, "kind": "reference",
                    "sample": f"{s} steps of the reference step loop on the {n}-node inlet section (96x40x96) of "
                              f"the tree, one process"}

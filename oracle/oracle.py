@@ -331,7 +331,7 @@ def ref_available(Q=19):
 
 def run_reference(stl_path, spacing, grid=None, preds=(), preset=None, tau=None, outlet_rho=None, steps=0,
                   profile=None, amp=None, inlet_dir=(0.0, -1.0, 0.0), Q=19, vtk_dir=None, workdir=None,
-                  flags_path=None):
+                  flags_path=None, warmup=0):
     """Runs the reference harness; returns its outputs as numpy arrays.  With
     flags_path the node-type field of the (explicit) grid is read from that file
     instead of the reference's voxelizer."""
@@ -355,6 +355,8 @@ def run_reference(stl_path, spacing, grid=None, preds=(), preset=None, tau=None,
     if outlet_rho is not None:
         lines.append(f"outlet_rho {outlet_rho!r}")
     lines.append(f"steps {steps}")
+    if warmup:
+        lines.append(f"warmup {int(warmup)}")
     lines.append("inlet_dir " + " ".join(repr(float(v)) for v in inlet_dir))
     if profile is not None:
         pp = os.path.join(wd, "profile.bin")

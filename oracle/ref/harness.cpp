@@ -22,6 +22,8 @@
 //                              list 0 = inlet, 1..6 = outlet lists 1..6
 //   vtk <dir>                  write the eight boundary-point VTK files there
 //   tau <t>   outlet_rho <r>   steps <n>
+//   warmup <n>                 untimed iterations before the <steps> timed ones
+//                              (the outputs are the state after all of them)
 //   inlet_dir <dx> <dy> <dz>   inlet_profile <file of doubles, one per inlet node>
 //   amp_table <file of doubles> amplitude a(t) = table[t mod len]; the inlet
 //                              velocity of node m at step t is (a*p_m)*dir
@@ -84,7 +86,7 @@ int main(int argc, char** argv) {
     std::ifstream run(argv[1]);
     std::string line, stl, out = "ref", vtkdir, profile_path, amp_path, flags_path;
     double spacing = 1.0, tau = 0.8, box[3] = {0, 0, 0};
-    int dims[3] = {0, 0, 0}, steps = 0;
+    int dims[3] = {0, 0, 0}, steps = 0, warmup = 0;
     bool have_box = false, preset = false;
     double idir[3] = {0.0, -1.0, 0.0};
     std::vector<Pred> preds;
@@ -108,6 +110,7 @@ int main(int argc, char** argv) {
         else if (key == "tau") ss >> tau;
         else if (key == "outlet_rho") ss >> g_oracle_outlet_rho;
         else if (key == "steps") ss >> steps;
+        else if (key == "warmup") ss >> warmup;
         else if (key == "inlet_dir") ss >> idir[0] >> idir[1] >> idir[2];
         else if (key == "inlet_profile") ss >> profile_path;
         else if (key == "amp_table") ss >> amp_path;
@@ -216,8 +219,7 @@ int main(int argc, char** argv) {
         std::fprintf(stderr, "inlet profile has %zu entries, inlet list %zu\n", profile.size(), D.InletBoundaryNode_.size());
         return 4;
     }
-    auto t2 = std::chrono::steady_clock::now();
-    for (int it = 0; it < steps; ++it) {
+    auto iterate = [&](int it) {
         if (!profile.empty()) {
             double a = amp[(size_t)it % amp.size()];
             for (size_t m = 0; m < D.InletBoundaryNode_.size(); ++m) {
@@ -230,7 +232,10 @@ int main(int argc, char** argv) {
         sim.ApplyZouHeBc();
         sim.ApplyWallBc();
         sim.ApplyOutletBc();
-    }
+    };
+    for (int it = 0; it < warmup; ++it) iterate(it);
+    auto t2 = std::chrono::steady_clock::now();
+    for (int it = warmup; it < warmup + steps; ++it) iterate(it);
     auto t3 = std::chrono::steady_clock::now();
     double secs = std::chrono::duration<double>(t3 - t2).count();
     std::fprintf(stderr, "steps: %d over %zu nodes, %.3f s, %.4f MLUPS\n", steps, D.Involved_Lat_.size(), secs,
