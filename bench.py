@@ -367,7 +367,7 @@ def main():
     ap.add_argument("--staging", type=int, default=1, help="0 = TMA-staged pipeline, 1 = direct loads")
     ap.add_argument("--nodes-per-lane", type=int, default=0, help="0 = engine default (paired), 1 or 2")
     ap.add_argument("--piece-slots", type=int, default=0, help="paired kernel: 8, 16 or 32 node slots per chunk "
-                                                                   "piece; 0 = engine default (16)")
+                                                                   "piece; 0 = engine default (8)")
     ap.add_argument("--err-steps", type=int, default=500)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the 64-vessel ensemble line")

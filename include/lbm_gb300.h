@@ -247,7 +247,7 @@ typedef struct lbm_sim_params {
     int32_t piece_slots;       /* two nodes per lane: node slots per chunk piece (8, 16 or 32;
                                   a piece is one run segment served by piece_slots/2 lanes,
                                   so shorter pieces leave fewer idle lanes at run ends and
-                                  read more descriptor bytes); 0 = default (16).  Results do
+                                  read more descriptor bytes); 0 = default (8).  Results do
                                   not depend on it. */
 } lbm_sim_params;
 

@@ -188,7 +188,7 @@ def test_piece_sizes_give_identical_results(precision, pattern):
 def test_piece_size_default_and_arguments():
     c = cases.pipe()
     geom = c.geometry()
-    assert Simulation(geom, c.tau, c.boundary_specs(geom), precision="f16s", pattern="aa").info().piece_slots == 16
+    assert Simulation(geom, c.tau, c.boundary_specs(geom), precision="f16s", pattern="aa").info().piece_slots == 8
     assert Simulation(geom, c.tau, c.boundary_specs(geom), precision="f64").info().piece_slots == 0
     for bad in (4, 12, 64, -1):
         with pytest.raises(_capi.LbmError) as e:
