@@ -231,9 +231,11 @@ __global__ void k_zflag(const int8_t* __restrict__ role, int64_t n, uint64_t zli
 }
 
 __global__ void k_gather_role(const int64_t* __restrict__ ids, int64_t n, const int8_t* __restrict__ role,
-                              int8_t* __restrict__ out) {
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+                              const int32_t* __restrict__ pos, int8_t* __restrict__ out, int32_t* __restrict__ out_pos) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         out[i] = role[ids[i]];
+        out_pos[i] = pos[ids[i]];
+    }
 }
 
 // per padded column (a, b): chunks (runs of fluid cells, <= 32) and boundary lanes
@@ -574,39 +576,51 @@ Vel make_vel(int Q, int ra) {
     return v;
 }
 
-// Number of chunks (fluid runs along the run axis, cut at 32) for a run axis.
-lbm_status count_chunks(const lbm_geometry* g, int ra, cudaStream_t st, int64_t* n) {
+// Chunk count of a run axis straight from the x-major fluid flags (no
+// permutation, no node typing): the fluid runs along the axis, each cut into
+// pieces of `piece` slots, widened to whole pairs of padded levels when
+// `pairs` (the paired kernel's pieces, k_col_count2); summed into *total.
+__global__ void k_count_runs(const uint8_t* __restrict__ flags, int Nx, int Ny, int Nz, int ra, int piece, int pairs,
+                             unsigned long long* __restrict__ total) {
+    const int64_t nb = ra == 2 ? Ny : Nz, len = ra == 2 ? Nz : Ny, stride = ra == 2 ? 1 : Nz;
+    const int64_t ncol = (int64_t)Nx * nb;
+    unsigned long long cnt = 0;
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncol; c += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t x = c / nb, b = c % nb;
+        const int64_t base = ra == 2 ? (x * Ny + b) * Nz : x * (int64_t)Ny * Nz + b;
+        int64_t rf = -1;
+        for (int64_t r = 0; r <= len; ++r) {
+            const bool fl = r < len && flags[base + r * stride] != 0;
+            if (fl && rf < 0) rf = r;
+            if (!fl && rf >= 0) {
+                int64_t lo = rf + 1, hi = r;                 // padded levels of the run
+                if (pairs) { lo &= ~int64_t(1); hi |= 1; }
+                cnt += (unsigned long long)((hi - lo + piece) / piece);
+                rf = -1;
+            }
+        }
+    }
+    for (int o = 16; o > 0; o >>= 1) cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(total, cnt);
+}
+
+// Number of chunks of the step kernel in use (paired pieces of `piece`
+// slots, or one-node chunks of at most 32 nodes) for a run axis.
+lbm_status count_chunks(const lbm_geometry* g, int ra, int piece, bool pairs, cudaStream_t st, int64_t* n) {
     int dims[3];
     geometry_dims(g, dims);
-    const Perm P{ra, dims[0], dims[1], dims[2]};
-    const int64_t npts = (int64_t)dims[0] * dims[1] * dims[2];
-    const uint8_t* flags = geometry_flags_dev(g);
-    DBuf<uint8_t> fp;
-    if (ra != 2) {
-        LBM_TRY(fp.alloc(npts, "permuted flags"));
-        k_permute_flags<<<blocks_for(npts, 256), 256, 0, st>>>(flags, P, fp.p);
-        flags = fp.p;
-    }
-    const Pad D{P.Na(), P.Nb(), P.Nr()};
-    DBuf<uint8_t> type;
-    LBM_TRY(type.alloc(D.cells(), "node types"));
-    LBM_TRY(compute_types(flags, D, type.p, st));
-    // chunks only depend on the fluid runs; roles are not needed: count with
-    // a role array of zeros via the fluid cells themselves
-    const int64_t ncol = (int64_t)D.Na * D.Nb;
-    std::vector<int32_t> dummy;
-    DBuf<int32_t> cc, bc, nocell;
-    DBuf<int8_t> zero;
-    DBuf<int64_t> co;
-    LBM_TRY(cc.alloc(ncol, "chunk counts"));
-    LBM_TRY(bc.alloc(ncol, "boundary counts"));
-    LBM_TRY(nocell.alloc(D.cells(), "node map"));
-    LBM_TRY(zero.alloc(1, "role"));
-    LBM_CUDA(cudaMemsetAsync(nocell.p, 0, sizeof(int32_t) * D.cells(), st));
-    LBM_CUDA(cudaMemsetAsync(zero.p, 0, 1, st));
-    LBM_TRY(co.alloc(ncol, "chunk offsets"));
-    k_col_count<<<blocks_for(ncol, 128), 128, 0, st>>>(type.p, nocell.p, zero.p, D, cc.p, bc.p);
-    return scan::exclusive_scan(cc.p, ncol, co.p, n, st);
+    DBuf<unsigned long long> tot;
+    LBM_TRY(tot.alloc(1, "chunk count"));
+    LBM_CUDA(cudaMemsetAsync(tot.p, 0, sizeof(unsigned long long), st));
+    const int64_t ncol = (int64_t)dims[0] * (ra == 2 ? dims[1] : dims[2]);
+    k_count_runs<<<blocks_for(ncol, 128), 128, 0, st>>>(geometry_flags_dev(g), dims[0], dims[1], dims[2], ra, piece,
+                                                          pairs ? 1 : 0, tot.p);
+    LBM_CUDA(cudaGetLastError());
+    unsigned long long h = 0;
+    LBM_CUDA(cudaMemcpyAsync(&h, tot.p, sizeof h, cudaMemcpyDeviceToHost, st));
+    LBM_CUDA(cudaStreamSynchronize(st));
+    *n = (int64_t)h;
+    return LBM_OK;
 }
 
 lbm_status build_instance(const lbm_geometry* g, const lbm_sim_params* p, int Q, int32_t inst, int ra, int npl,
@@ -679,18 +693,19 @@ lbm_status build_instance(const lbm_geometry* g, const lbm_sim_params* p, int Q,
         // profile values follow the list's x-major order (the reference's
         // InletBoundaryNode_ order); slots follow the internal node order
         DBuf<int8_t> zr;
+        DBuf<int32_t> zp;
         LBM_TRY(zr.alloc(nzn, "zou-he roles"));
-        if (nzn) k_gather_role<<<blocks_for(nzn, 256), 256, 0, st>>>(zn, nzn, role.p, zr.p);
+        LBM_TRY(zp.alloc(nzn, "zou-he output positions"));
+        if (nzn)
+            k_gather_role<<<blocks_for(nzn, 256), 256, 0, st>>>(zn, nzn, role.p, out.out_pos.p, zr.p, zp.p);
         std::vector<int8_t> hr(nzn);
         std::vector<int64_t> hid(nzn);
         if (nzn) {
-            std::vector<int32_t> pos(out.N);
-            std::vector<int64_t> ids(nzn);
+            std::vector<int32_t> pos(nzn);
             LBM_CUDA(cudaMemcpyAsync(hr.data(), zr.p, nzn, cudaMemcpyDeviceToHost, st));
-            LBM_CUDA(cudaMemcpyAsync(pos.data(), out.out_pos.p, sizeof(int32_t) * out.N, cudaMemcpyDeviceToHost, st));
-            LBM_CUDA(cudaMemcpyAsync(ids.data(), zn, sizeof(int64_t) * nzn, cudaMemcpyDeviceToHost, st));
+            LBM_CUDA(cudaMemcpyAsync(pos.data(), zp.p, sizeof(int32_t) * nzn, cudaMemcpyDeviceToHost, st));
             LBM_CUDA(cudaStreamSynchronize(st));
-            for (int64_t s = 0; s < nzn; ++s) hid[s] = pos[ids[s]];
+            for (int64_t s = 0; s < nzn; ++s) hid[s] = pos[s];
         }
         std::vector<int64_t> order(nzn);
         for (int64_t s = 0; s < nzn; ++s) order[s] = s;
@@ -942,8 +957,9 @@ lbm_status sim_create(const lbm_geometry* const* g, const lbm_sim_params* p, siz
         int64_t cy = 0, cz = 0;
         for (size_t i = 0; i < n; ++i) {
             int64_t a = 0, b = 0;
-            LBM_TRY(count_chunks(g[i], 1, st, &a));
-            LBM_TRY(count_chunks(g[i], 2, st, &b));
+            const bool pairs = S->npl == 2;
+            LBM_TRY(count_chunks(g[i], 1, pairs ? S->piece : 32, pairs, st, &a));
+            LBM_TRY(count_chunks(g[i], 2, pairs ? S->piece : 32, pairs, st, &b));
             cy += a;
             cz += b;
         }
