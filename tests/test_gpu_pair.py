@@ -194,3 +194,19 @@ def test_piece_size_default_and_arguments():
         with pytest.raises(_capi.LbmError) as e:
             Simulation(geom, c.tau, c.boundary_specs(geom), precision="f16s", pattern="aa", piece_slots=bad)
         assert e.value.status == _capi.ERR_ARG
+
+
+@pytest.mark.parametrize("make", [cases.pipe, lambda: cases.vessel(4006), lambda: cases.vessel(4008)])
+def test_automatic_run_axis_has_fewer_chunks(make):
+    """run_axis = 0 takes the axis whose chunk table is shorter: the count
+    comes straight from the voxel flags and must agree with the tables the
+    lattice builder makes for either axis."""
+    c = make()
+    geom = c.geometry()
+    specs = c.boundary_specs(geom)
+    n = {}
+    for ra in (1, 2):
+        n[ra] = Simulation(geom, c.tau, specs, precision="f16s", pattern="aa", run_axis=ra).info().n_chunks
+    auto = Simulation(geom, c.tau, specs, precision="f16s", pattern="aa").info()
+    assert auto.n_chunks == min(n.values())
+    assert n[auto.run_axis] == auto.n_chunks
