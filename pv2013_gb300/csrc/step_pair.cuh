@@ -263,8 +263,9 @@ __device__ __forceinline__ void collide2(const typename PairWord<S>::W* raw, flo
 // register budget per thread (measured on the vascular tree): D3Q19 with
 // 16-bit storage holds one 32-bit word per population; 64 registers for the
 // node-local and pull patterns, 72 for the AA odd pattern (its scatter needs a
-// few more; 72 keeps 28 warps per SM and removes the spills of a 64 budget);
-// FP32 storage (two registers per word) and D3Q27 get 128.
+// few more; 72 keeps 28 warps per SM and leaves a few bytes of spills where
+// 64 spilled ~150 B; faster than both 64 and 80); FP32 storage (two
+// registers per word) and D3Q27 get 128.
 template <int Q, int S, int MODE> struct PairMaxReg {
     static constexpr int value = (Q == 19 && S != ST_F32) ? (MODE == MODE_AA_ODD ? 72 : 64) : 128;
 };
