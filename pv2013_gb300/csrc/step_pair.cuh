@@ -357,19 +357,16 @@ __global__ void __launch_bounds__(256) __maxnreg__((PairMaxReg<Q, S, MODE>::valu
     }
 
     // L2 prefetch of that piece's window in every plane: lane t of the piece's
-    // lane group takes planes t, t + 2^lg, ... (words n0/2 - 1 and n0/2 + 2^lg,
-    // the ends of the window with its straddle words).  Neighbour columns'
-    // windows are the windows of nearby pieces, prefetched by them.  Ids
-    // stay in [8, N - 8), so both words lie inside the population array.
+    // lane group takes planes t, t + 2^lg, ..., one prefetch at the window's
+    // first word (an 8-slot window is 16 B; a second prefetch at its end
+    // measured 2 % slower).  Neighbour columns' windows are the windows of
+    // nearby pieces, prefetched by them.  Ids stay in [8, N - 8), so the word
+    // lies inside the population array.
     if (hfp) {
-        const uint32_t wf = nfp >> 1, wl = wf + (1u << lg);
+        const uint32_t wf = nfp >> 1;
         const char* Ab = reinterpret_cast<const char*>(A);
-        for (int q = t; q < Q; q += 1 << lg) {
-            const char* p0 = Ab + (size_t)((uint32_t)q * sw + wf - 1u) * sizeof(W);
-            const char* p1 = Ab + (size_t)((uint32_t)q * sw + wl) * sizeof(W);
-            asm volatile("prefetch.global.L2 [%0];" ::"l"(p0));
-            asm volatile("prefetch.global.L2 [%0];" ::"l"(p1));
-        }
+        for (int q = t; q < Q; q += 1 << lg)
+            asm volatile("prefetch.global.L2 [%0];" ::"l"(Ab + (size_t)((uint32_t)q * sw + wf) * sizeof(W)));
     }
     // the odd pattern's column bases go through shared memory (lane 0 of
     // each chunk wrote them): fewer registers held across the collision
