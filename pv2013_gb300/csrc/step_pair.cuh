@@ -285,8 +285,9 @@ __global__ void __launch_bounds__(256) __maxnreg__((PairMaxReg<Q, S, MODE>::valu
     // chunk descriptor words 0-7 (n0, len_inst, wmask, zmask, bmask, zslot0, mslot0, K0)
     const uint4* cw = reinterpret_cast<const uint4*>(a.chunks + (have_chunk ? ci : 0));
     const uint4 d0 = have_chunk ? __ldg(cw) : make_uint4(0u, 0u, 0u, 0u);
-    // start id of the piece one wave of resident warps ahead: its population
-    // windows are prefetched into L2 below (the load is in flight with d0)
+    // start id of the piece half a wave of resident warps ahead: its
+    // population windows are prefetched into L2 below (the load is in flight
+    // with d0)
     const int64_t cfp = ci + a.pf_ahead;
     const bool hfp = a.pf_ahead > 0 && cfp < a.nchunks;
     uint32_t nfp = 0;
@@ -468,7 +469,7 @@ static lbm_status launch_pair_one(const StepArgs& a, int wpb, cudaStream_t st) {
     }
     const int64_t per_block = (int64_t)wpb << (5 - a.piece_lg);
     const int64_t blocks = (a.nchunks + per_block - 1) / per_block;
-    // prefetch distance: the pieces of one wave of resident blocks
+    // prefetch distance: in pieces, from the blocks resident at once
     static int resident[9] = {0};
     if (resident[wpb] == 0) {
         int dev = 0, sms = 0, nb = 0;
@@ -478,8 +479,9 @@ static lbm_status launch_pair_one(const StepArgs& a, int wpb, cudaStream_t st) {
             return fail(LBM_ERR_CUDA, "paired step kernel occupancy: %s", cudaGetErrorString(cudaGetLastError()));
         resident[wpb] = sms * (nb > 0 ? nb : 1);
     }
+    // half a wave ahead: measured 0.4 % faster than one wave, 1.5 % faster than 1.5 waves
     StepArgs b = a;
-    b.pf_ahead = (int64_t)resident[wpb] * per_block;
+    b.pf_ahead = (int64_t)resident[wpb] * per_block / 2;
     k_step2<Q, S, MODE, RA><<<(unsigned)(blocks > 0 ? blocks : 1), 32 * wpb, smem, st>>>(b);
     return LBM_OK;
 }
