@@ -459,29 +459,34 @@ template <int Q, int S, int MODE, int RA>
 static lbm_status launch_pair_one(const StepArgs& a, int wpb, cudaStream_t st) {
     // dynamic shared memory: one word per population and lane of each warp
     // (the Zou-He path); above 48 KB it needs the opt-in attribute
-    static int opted = 0;
+    // per-device caches (written with the same value by any thread that
+    // fills them): the shared-memory opt-in and the blocks resident at once
+    constexpr int kDevs = 16;
+    static int opted[kDevs] = {0};
+    static int resident[kDevs][9] = {{0}};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kDevs)
+        return fail(LBM_ERR_CUDA, "paired step kernel: device %d not supported", dev);
     const size_t smem = (size_t)wpb * Q * 32 * sizeof(typename PairWord<S>::W);
-    if (smem > 48 * 1024 && opted < (int)smem) {
+    if (smem > 48 * 1024 && opted[dev] < (int)smem) {
         const cudaError_t e = cudaFuncSetAttribute(k_step2<Q, S, MODE, RA>,
                                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return fail(LBM_ERR_CUDA, "paired step kernel shared memory: %s", cudaGetErrorString(e));
-        opted = (int)smem;
+        opted[dev] = (int)smem;
     }
     const int64_t per_block = (int64_t)wpb << (5 - a.piece_lg);
     const int64_t blocks = (a.nchunks + per_block - 1) / per_block;
     // prefetch distance: in pieces, from the blocks resident at once
-    static int resident[9] = {0};
-    if (resident[wpb] == 0) {
-        int dev = 0, sms = 0, nb = 0;
-        if (cudaGetDevice(&dev) != cudaSuccess ||
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+    if (resident[dev][wpb] == 0) {
+        int sms = 0, nb = 0;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_step2<Q, S, MODE, RA>, 32 * wpb, smem) != cudaSuccess)
             return fail(LBM_ERR_CUDA, "paired step kernel occupancy: %s", cudaGetErrorString(cudaGetLastError()));
-        resident[wpb] = sms * (nb > 0 ? nb : 1);
+        resident[dev][wpb] = sms * (nb > 0 ? nb : 1);
     }
     // half a wave ahead: measured 0.4 % faster than one wave, 1.5 % faster than 1.5 waves
     StepArgs b = a;
-    b.pf_ahead = (int64_t)resident[wpb] * per_block / 2;
+    b.pf_ahead = (int64_t)resident[dev][wpb] * per_block / 2;
     k_step2<Q, S, MODE, RA><<<(unsigned)(blocks > 0 ? blocks : 1), 32 * wpb, smem, st>>>(b);
     return LBM_OK;
 }
