@@ -91,7 +91,9 @@ public:
         : velSet_(std::move(velSet)), spacing(spacing), maxDepth(mdepth) {
         lbm_tri* tris = nullptr;
         size_t n = 0;
-        check(lbm_stl_read_ascii(FileName.c_str(), &tris, &n));
+        // parsed on the GPU (the same triangles as the host reader, which takes
+        // over for files outside the canonical facet layout)
+        check(lbm_stl_read_ascii_device(FileName.c_str(), nullptr, &tris, &n, nullptr));
         std::unique_ptr<lbm_tri, void (*)(void*)> hold(tris, lbm_free);
         if (preds.empty()) {
             size_t np = 0;
