@@ -253,16 +253,26 @@ extern "C" lbm_status lbm_stl_read_ascii_device(const char* path, void* stream, 
         std::fclose(fh);
         return fail(LBM_ERR_IO, "cannot size file %s", path);
     }
+    // pinned host memory for the copy to the device; ordinary memory when
+    // pinning that much fails (the copy is then slower, the result the same)
     char* text = nullptr;
-    if (cudaMallocHost(&text, (size_t)(sz > 0 ? sz : 1)) != cudaSuccess) {
-        std::fclose(fh);
+    bool pinned = cudaMallocHost(&text, (size_t)(sz > 0 ? sz : 1)) == cudaSuccess;
+    if (!pinned) {
         cudaGetLastError();
-        return fail(LBM_ERR_NOMEM, "cannot pin %ld bytes for %s", sz, path);
+        text = (char*)std::malloc((size_t)(sz > 0 ? sz : 1));
+        if (!text) {
+            std::fclose(fh);
+            return fail(LBM_ERR_NOMEM, "cannot hold %ld bytes of %s", sz, path);
+        }
     }
+    auto release = [&]() {
+        if (pinned) cudaFreeHost(text);
+        else std::free(text);
+    };
     const size_t got = sz > 0 ? std::fread(text, 1, (size_t)sz, fh) : 0;
     std::fclose(fh);
     if (got != (size_t)sz) {
-        cudaFreeHost(text);
+        release();
         return fail(LBM_ERR_IO, "short read of %s", path);
     }
     bool ok = false;
@@ -270,7 +280,7 @@ extern "C" lbm_status lbm_stl_read_ascii_device(const char* path, void* stream, 
     // NUL bytes end the host tokenizer's lines early: host grammar
     if (!std::memchr(text, 0, (size_t)sz))
         s = parse_on_device(text, (int64_t)sz, (cudaStream_t)stream, tris, n, &ok);
-    cudaFreeHost(text);
+    release();
     if (s != LBM_OK) return s;
     if (ok) {
         if (on_device) *on_device = 1;
