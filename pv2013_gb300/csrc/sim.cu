@@ -917,8 +917,8 @@ lbm_status sim_create(const lbm_geometry* const* g, const lbm_sim_params* p, siz
     if (S->store < 0) return fail(LBM_ERR_ARG, "unknown precision %d", p0.precision);
     S->pattern = p0.pattern == LBM_AUTO ? LBM_AA : p0.pattern;
     if (S->pattern != LBM_PULL && S->pattern != LBM_AA) return fail(LBM_ERR_ARG, "unknown pattern %d", p0.pattern);
-    // default block: 4 warps for the one-node-per-lane kernels, 1 warp (two
-    // chunks) for the paired kernel (measured on the vascular tree)
+    // default block: 4 warps for the one-node-per-lane kernels, 1 warp (its
+    // chunk pieces) for the paired kernel (measured on the vascular tree)
     S->wpb = p0.warps_per_block > 0 ? p0.warps_per_block : 0;
     if (S->wpb > 8) return fail(LBM_ERR_ARG, "warps_per_block must be <= 8");
     if (p0.run_axis != 0 && p0.run_axis != 1 && p0.run_axis != 2) return fail(LBM_ERR_ARG, "run_axis must be 0, 1 or 2");
