@@ -170,3 +170,16 @@ def test_device_stl_reader_without_device_fails_cleanly(tmp_path):
     with pytest.raises(_capi.LbmError) as e:
         Reader.readSTLASCIIDevice(p)
     assert e.value.status == 9
+
+
+def test_prototypes_have_the_header_argument_counts():
+    """Each ctypes prototype takes as many arguments as the header declares."""
+    decl = {}
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = re.sub(r"/\*.*?\*/", "", open(h).read(), flags=re.S)
+        for m in re.finditer(r"\b(lbm_[a-z0-9_]+)\s*\(([^()]*)\)\s*;", text):
+            params = m.group(2).strip()
+            decl[m.group(1)] = 0 if params in ("", "void") else params.count(",") + 1
+    assert len(decl) >= 25
+    for name, n in decl.items():
+        assert len(_capi.PROTOTYPES[name][1]) == n, name
