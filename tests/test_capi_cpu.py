@@ -140,6 +140,20 @@ def test_synthetic_meshes_are_closed(make):
     assert np.allclose(np.linalg.norm(n, axis=1), 1.0)
 
 
+def test_benchmark_tree_is_reproducible():
+    """The seeded benchmark workload is the same mesh on every build: the
+    tree's triangle count and an order-dependent checksum of its bytes are
+    stable across calls (the bench's grid, fluid-node count and outlet lists
+    follow from it)."""
+    import hashlib
+    a, b = cases.vascular_tree(h=2.2), cases.vascular_tree(h=2.2)
+    assert len(a.triangles) == len(b.triangles) == 2066396
+    ha = hashlib.sha256(np.ascontiguousarray(a.triangles).tobytes()).hexdigest()
+    hb = hashlib.sha256(np.ascontiguousarray(b.triangles).tobytes()).hexdigest()
+    assert ha == hb
+    assert a.triangles.shape[1] == 12
+
+
 def test_pv2013_predicates_hold_reference_constants():
     preds = pv2013_gb300.pv2013_predicates()
     planes = ["-175.275", "-164.075", "-174.475", "-28.3", "-25.5", "-37.0", "-108.379"]
