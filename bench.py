@@ -211,8 +211,7 @@ def reference_arm(args):
 def gpu_arm(args, rank, world):
     import numpy as np
     import torch
-    from pv2013_gb300 import Reader, Simulation, cases
-    from pv2013_gb300 import engine as E
+    from pv2013_gb300 import Simulation, cases
     dev = int(os.environ.get("LOCAL_RANK", "0"))
     torch.cuda.set_device(dev)
     torch.cuda.init()

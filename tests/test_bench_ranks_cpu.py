@@ -5,7 +5,6 @@ import os
 import socket
 import sys
 
-import pytest
 import torch.multiprocessing as mp
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
@@ -18,7 +17,6 @@ def _free_port():
 
 
 def _worker(rank, world, port, out):
-    import torch
     import torch.distributed as dist
     sys.path.insert(0, ROOT)
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))

@@ -2,7 +2,6 @@
 exports every entry point declared in include/*.h, STL I/O follows the
 reference reader's grammar, the synthetic meshes are closed surfaces and the
 PV2013 predicate preset holds the reference's constants."""
-import ctypes as C
 import glob
 import os
 import re

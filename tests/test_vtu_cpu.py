@@ -1,5 +1,4 @@
 """The .vtu writer (lbm_vtu_write): XML header, appended raw blocks, values."""
-import re
 import struct
 import xml.etree.ElementTree as ET
 
