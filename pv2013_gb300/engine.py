@@ -300,7 +300,13 @@ class Simulation:
     """Device lattice + time stepping (SubDomain + Simulation of the reference).
 
     ``geometry`` may be a Geometry or a list of them (batched ensemble, then
-    ``tau`` and ``bcs`` may be per-instance lists).
+    ``tau`` and ``bcs`` may be per-instance lists).  The keyword arguments are
+    the fields of ``lbm_sim_params``: ``precision`` (f64, f32, f16s, bf16s),
+    ``pattern`` (pull, aa), ``nodes_per_lane`` (0 = 2 for FP32/16-bit
+    storage, 1 for FP64), ``piece_slots`` (8, 16, 32; 0 = 8),
+    ``warps_per_block``, ``run_axis`` (0 = the axis with fewer chunks),
+    ``staging`` (one node per lane: 0 TMA ring, 1 direct loads) and
+    ``corrections`` (``_capi.FIX_*`` bits; 0 = the reference's behaviour).
     """
 
     def __init__(self, geometry, tau, bcs=(), Q=19, precision="f64", pattern="pull", warps_per_block=0, run_axis=0,
