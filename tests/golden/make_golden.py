@@ -1,8 +1,8 @@
 #!/usr/bin/env python3
 """Generates the PV2013 golden fixtures from the reference checkout.
 
-Inputs (read from the reference directory given as argv[1], default
-/root/reference):
+Inputs (read from the reference checkout given as argv[1], or else by the
+PV2013_REF_DIR environment variable):
   PV2013.stl                                  the vessel surface (ASCII STL)
   InboundaryPointsFromGeometry.vtk,
   OutboundaryPointsFromGeometry{1..6}.vtk,
@@ -35,7 +35,9 @@ KEYS = ["inlet"] + [f"outlet{k}" for k in range(1, 7)] + ["wall"]
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PV2013_REF_DIR")
+    if not ref:
+        raise SystemExit("usage: make_golden.py REFERENCE_DIR (or set PV2013_REF_DIR)")
     from oracle import oracle as O
     tris = O.read_stl_ascii(os.path.join(ref, "PV2013.stl"))
     np.savez_compressed(os.path.join(HERE, "pv2013_tris.npz"), tris=tris)
