@@ -24,6 +24,14 @@
 // DRY launches run the gather and boundary part only and write f_n, rho_n,
 // u_n in FP64 (snapshots and monitors); they never modify the state.
 //
+// Missing populations in the AA pattern (source node x - c_q absent): the
+// AA odd launch stores, for an absent x + c_q, f*_q (bounced) or the initial
+// value (where the reference never writes the population: direction 0 of its
+// wall loop, inlet/outlet nodes; see bounce_back_pop) in slot opp(q) of x,
+// which is where the next AA even launch reads population opp(q): that
+// launch needs no fix-up.  The AA odd launch takes a missing population from
+// the node's own slot q (the even launch left f*_opp(q) there) or resets it.
+//
 // Neighbour addressing: on the ghost-padded run lattice (device.cuh) the
 // source of population q of lane t is K[column] + const + t, one integer add;
 // boundary lanes read a precomputed mask of their missing populations.
@@ -283,6 +291,21 @@ __device__ __forceinline__ void zou_he_apply(T* p, int kind, int face, const T* 
     }
 }
 
+// Whether boundary node population p (its source absent) takes the bounced
+// value f*_opp(p) or keeps the initial value: wall nodes bounce back every
+// population but opp(0) of D3Q19 (ApplyWallBc loops dir = 1..Q-1,
+// Simulation.cpp:1361); inlet/outlet nodes keep the initial value (their
+// Zou-He routine rewrites the unknowns); LBM_FIX_* widen both.
+template <int Q>
+__device__ __forceinline__ bool bounce_back_pop(int p, bool wall, uint32_t corr) {
+    return (wall || (corr & LBM_FIX_LIST_NODES)) && (p != Lat<Q>::NO_BB_POP || (corr & LBM_FIX_BB_ALL_DIRS));
+}
+// initial value of population q as a working value (node_update's reset)
+template <int S, int Q>
+__device__ __forceinline__ typename Work<S>::T init_work(int q) {
+    return S == ST_F64 ? typename Work<S>::T(Lat<Q>::w(q)) : typename Work<S>::T(0);
+}
+
 __host__ __device__ constexpr bool is_velocity_kind(int kind) {
     return kind == LBM_BC_VEL_NEGY || kind == LBM_BC_VEL_POSX || kind == LBM_BC_VELOCITY;
 }
@@ -486,13 +509,13 @@ __global__ void __launch_bounds__(256, 4) k_step(StepArgs a, Partials part) {
         const int len = (int)(li & 63u);
         if (lane < len) {
             const uint32_t wmask = __ldg(&cp->wmask), zmask = __ldg(&cp->zmask), bmask = __ldg(&cp->bmask);
+            const int32_t n = n0 + lane;
+            const uint32_t missing = lane_missing(a, cp, bmask, lane);
             int32_t K[8];
             if constexpr (MODE != MODE_AA_EVEN) {
 #pragma unroll
                 for (int c = 0; c < 8; ++c) K[c] = __ldg(&cp->K[c]);
             }
-            const int32_t n = n0 + lane;
-            const uint32_t missing = lane_missing(a, cp, bmask, lane);
             const int64_t step = a.step + (a.step_base ? *a.step_base : 0);
             T f[Q];
             const void* A = a.src;
@@ -520,14 +543,16 @@ __global__ void __launch_bounds__(256, 4) k_step(StepArgs a, Partials part) {
                     } else if constexpr (MODE == MODE_AA_EVEN) {
                         st<S, Q>(D, a.stride, L::opp(q), n, f[q]);
                     } else {
-                        // branch-free: an absent destination receives the value in the
-                        // node's own opposite slot
+                        // branch-free: an absent destination receives the value (bounced
+                        // or initial) in the node's own opposite slot
                         if (q == 0) {
 #pragma unroll
                             for (int c = 0; c < 8; ++c) K[c] = ld_fresh(&cp->K[c]);
                         }
                         const bool back = (missing >> L::opp(q)) & 1u;
-                        st_sel<S, Q>(D, (uint32_t)a.stride, q, nb_id(K, n0, lane, X::a(q), X::b(q), X::r(q)), back, n, f[q]);
+                        const bool keep = !back || bounce_back_pop<Q>(L::opp(q), (wmask >> lane) & 1u, a.corr);
+                        st_sel<S, Q>(D, (uint32_t)a.stride, q, nb_id(K, n0, lane, X::a(q), X::b(q), X::r(q)), back, n,
+                                     keep ? f[q] : init_work<S, Q>(q));
                     }
                 }
             }

@@ -14,6 +14,11 @@
 //   * the collision runs on packed FP32 pairs (add/sub/mul/fma.rn.f32x2), one
 //     instruction for both nodes;
 //   * boundary fix-ups and Zou-He run per node, only in warps that have them.
+//     The AA even launch has no fix-ups: the odd launch before it left the
+//     bounced or initial values in the node's own slots (step_kernel.cuh).
+//     The AA odd launch's bounce-back source is the node's own word: boundary
+//     lanes copy their own words into shared memory (cp.async) while the
+//     gathers are in flight, so the fix-up waits on no further load.
 // Chunk pieces start at even levels and hold up to 8, 16 or 32 node slots
 // (lbm_sim_params.piece_slots: shorter pieces leave fewer idle lanes where a
 // run ends, for 64 descriptor bytes per piece); a slot at either end may be a
@@ -195,6 +200,8 @@ __device__ __forceinline__ void zou_he_half(const StepArgs& a, int slot, typenam
     for (int q = 0; q < Q; ++q) raw[q * 32] = set_half_plain<S, Q>(raw[q * 32], hi, p[q], q);
 }
 
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
 // identity the compiler cannot see through: the relaxation unpacks the words
 // again instead of keeping the first unpacked values alive
 __device__ __forceinline__ uint32_t opaque(uint32_t x) {
@@ -260,12 +267,10 @@ __device__ __forceinline__ void collide2(const typename PairWord<S>::W* raw, flo
     }
 }
 
-// register budget per thread (measured on the vascular tree): D3Q19 with
-// 16-bit storage holds one 32-bit word per population; 64 registers for the
-// node-local and pull patterns, 72 for the AA odd pattern (its scatter needs a
-// few more; 72 keeps 28 warps per SM and leaves a few bytes of spills where
-// 64 spilled ~150 B; faster than both 64 and 80); FP32 storage (two
-// registers per word) and D3Q27 get 128.
+// register budget per thread: D3Q19 with 16-bit storage holds one 32-bit
+// word per population; 64 registers for the node-local and pull patterns, 72
+// for the AA odd pattern (its scatter needs a few more; 72 keeps 28 warps per
+// SM); FP32 storage (two registers per word) and D3Q27 get 128.
 template <int Q, int S, int MODE> struct PairMaxReg {
     static constexpr int value = (Q == 19 && S != ST_F32) ? (MODE == MODE_AA_ODD ? 72 : 64) : 128;
 };
@@ -332,6 +337,10 @@ __global__ void __launch_bounds__(256) __maxnreg__((PairMaxReg<Q, S, MODE>::valu
 
     W raw[Q];
     __shared__ int32_t ksm[8][8][8];     // column bases of each warp's chunks
+    // the warp's shared words: the AA odd launch's bounce-back sources, then
+    // the Zou-He path's staging (one word per population and lane)
+    extern __shared__ __align__(16) unsigned char zsm[];
+    W* buf = (W*)zsm + (threadIdx.x >> 5) * (Q * 32) + lane;
     if (act) {
         int32_t K[8];
         if constexpr (MODE != MODE_AA_EVEN) load_K(K, false);
@@ -339,6 +348,17 @@ __global__ void __launch_bounds__(256) __maxnreg__((PairMaxReg<Q, S, MODE>::valu
             if (t == 0) {
 #pragma unroll
                 for (int c = 0; c < 8; ++c) ksm[threadIdx.x >> 5][pw][c] = K[c];
+            }
+            // boundary lanes: own words (slot q holds f*_opp(q) of the even
+            // launch, the bounce-back value of population q), in flight with
+            // the gathers
+            if ((bm_all >> (2 * t)) & 3u) {
+#pragma unroll
+                for (int q = 0; q < Q; ++q)
+                    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;" ::"r"(smem_u32(buf + q * 32)),
+                                 "l"(reinterpret_cast<const W*>(A) + ((uint32_t)q * sw + ew)), "n"(sizeof(W))
+                                 : "memory");
+                asm volatile("cp.async.commit_group;" ::: "memory");
             }
         }
 #pragma unroll
@@ -372,8 +392,46 @@ __global__ void __launch_bounds__(256) __maxnreg__((PairMaxReg<Q, S, MODE>::valu
     // the odd pattern's column bases go through shared memory (lane 0 of
     // each chunk wrote them): fewer registers held across the collision
     if constexpr (MODE == MODE_AA_ODD) __syncwarp();
-    // missing populations (boundary nodes): bounce-back or the initial value
-    if (__any_sync(0xffffffffu, (m_lo | m_hi) != 0u)) {
+    // AA odd: missing populations (boundary nodes) take the bounced value from
+    // the node's own word or the initial value (bounce_back_pop); only the
+    // populations missing somewhere in the warp are visited
+    if constexpr (MODE == MODE_AA_ODD) {
+        // every lane that issued own-word copies waits for them here, before
+        // the buffer is read or reused (a boundary node may miss no population)
+        if (__any_sync(0xffffffffu, ((bm_all >> (2 * t)) & 3u) != 0u)) {
+            asm volatile("cp.async.wait_all;" ::: "memory");
+            __syncwarp();
+        }
+        const uint32_t umiss = __reduce_or_sync(0xffffffffu, m_lo | m_hi);
+        if (umiss) {
+            uint32_t wm = 0u;
+            if (act) asm volatile("ld.global.nc.u32 %0, [%1];" : "=r"(wm) : "l"(&cw[0].z));   // wmask, read late
+            wm = (wm >> (2 * t)) & 3u;
+            // populations each node bounces back (the others take the initial value)
+            uint32_t keep = ~0u;
+            if (L::NO_BB_POP >= 0 && !(a.corr & LBM_FIX_BB_ALL_DIRS)) keep = ~(1u << (L::NO_BB_POP & 31));
+            const bool fix_list = a.corr & LBM_FIX_LIST_NODES;
+            const uint32_t b_lo = ((wm & 1u) || fix_list) ? (m_lo & keep) : 0u;
+            const uint32_t b_hi = ((wm & 2u) || fix_list) ? (m_hi & keep) : 0u;
+#pragma unroll
+            for (int q = 0; q < Q; ++q) {
+                if (!((umiss >> q) & 1u)) continue;
+                const bool bl = (b_lo >> q) & 1u, bh = (b_hi >> q) & 1u;
+                const bool il = ((m_lo & ~b_lo) >> q) & 1u, ih = ((m_hi & ~b_hi) >> q) & 1u;
+                if (bl || bh) {
+                    const W own = buf[q * 32];
+                    if (bl) raw[q] = take_half<S>(raw[q], false, own);
+                    if (bh) raw[q] = take_half<S>(raw[q], true, own);
+                }
+                if (il) raw[q] = init_half<S, Q>(raw[q], false, q);
+                if (ih) raw[q] = init_half<S, Q>(raw[q], true, q);
+            }
+            __syncwarp();
+        }
+    }
+    // pull: missing populations (boundary nodes) bounce back from slot opp(q)
+    // of the source lattice or take the initial value
+    if (MODE == MODE_PULL && __any_sync(0xffffffffu, (m_lo | m_hi) != 0u)) {
         uint32_t wm = 0u;
         if (act) asm volatile("ld.global.nc.u32 %0, [%1];" : "=r"(wm) : "l"(&cw[0].z));   // wmask, read late
         wm = (wm >> (2 * t)) & 3u;
@@ -386,15 +444,12 @@ __global__ void __launch_bounds__(256) __maxnreg__((PairMaxReg<Q, S, MODE>::valu
             if (ml || mh) {
                 const bool dir_ok = q != L::NO_BB_POP || all_dirs;
                 const bool bl = ml && w_lo && dir_ok, bh = mh && w_hi && dir_ok;
-                if constexpr (MODE != MODE_AA_EVEN) {
-                    // bounce-back source: own node, slot opp(q) (pull) or slot q (AA
-                    // odd); a predicated load and selects instead of branches
-                    W own = raw[q];
-                    if (bl || bh) own = ldw<S>(A, (uint32_t)(MODE == MODE_PULL ? L::opp(q) : q) * sw + ew);
-                    raw[q] = take_half<S>(raw[q], false, bl ? own : raw[q]);
-                    raw[q] = take_half<S>(raw[q], true, bh ? own : raw[q]);
-                }
-                // AA even: slot q of x already holds f*_{opp q}(x)
+                // bounce-back source: own node, slot opp(q) of the source lattice;
+                // a predicated load and selects instead of branches
+                W own = raw[q];
+                if (bl || bh) own = ldw<S>(A, (uint32_t)L::opp(q) * sw + ew);
+                raw[q] = take_half<S>(raw[q], false, bl ? own : raw[q]);
+                raw[q] = take_half<S>(raw[q], true, bh ? own : raw[q]);
                 if (ml && !bl) raw[q] = init_half<S, Q>(raw[q], false, q);
                 if (mh && !bh) raw[q] = init_half<S, Q>(raw[q], true, q);
             }
@@ -404,8 +459,6 @@ __global__ void __launch_bounds__(256) __maxnreg__((PairMaxReg<Q, S, MODE>::valu
     const uint32_t zm = (zm_all >> (2 * t)) & 3u;
     if (__any_sync(0xffffffffu, zm != 0u && step > 0)) {
         // the warp's words go through shared memory around the per-node update
-        extern __shared__ __align__(16) unsigned char zsm[];
-        W* buf = (W*)zsm + (threadIdx.x >> 5) * (Q * 32) + lane;
 #pragma unroll
         for (int q = 0; q < Q; ++q) buf[q * 32] = raw[q];
         if (step > 0 && zm) {
@@ -427,10 +480,14 @@ __global__ void __launch_bounds__(256) __maxnreg__((PairMaxReg<Q, S, MODE>::valu
         collide2<Q, S>(raw, om, [&](int q, F2 v) { stw<S>(D, (uint32_t)L::opp(q) * sw + ew, pack<S, Q>(v, q)); });
     } else {
         // AA odd: f*_q to slot q of x + c_q, or (absent destination) to slot
-        // opp(q) of x; ghost slots of the pair store nothing
-        uint32_t vm;
+        // opp(q) of x, there f*_q or the initial value (bounce_back_pop);
+        // ghost slots of the pair store nothing
+        uint32_t vm, wm = 0u;
         asm volatile("ld.global.nc.u32 %0, [%1];" : "=r"(vm) : "l"(&cw[3].w));
+        if (__any_sync(__activemask(), (m_lo | m_hi) != 0u))
+            asm volatile("ld.global.nc.u32 %0, [%1];" : "=r"(wm) : "l"(&cw[0].z));   // wmask
         vm = (vm >> (2 * t)) & 3u;
+        wm = (wm >> (2 * t)) & 3u;
         const volatile int32_t* ks = ksm[threadIdx.x >> 5][pw];
         // whole-word stores of the directions without a run-axis component
         // only when no lane of the warp has a ghost slot or a bounce-back
@@ -446,6 +503,8 @@ __global__ void __launch_bounds__(256) __maxnreg__((PairMaxReg<Q, S, MODE>::valu
             } else {
                 float l, h;
                 f2split(v, l, h);
+                if (bl && !bounce_back_pop<Q>(L::opp(q), wm & 1u, a.corr)) l = 0.f;
+                if (bh && !bounce_back_pop<Q>(L::opp(q), (wm >> 1) & 1u, a.corr)) h = 0.f;
                 if (vm & 1u) st_one<S, Q>(D, bl ? po + e : pq + s + o, l, q);
                 if (vm & 2u) st_one<S, Q>(D, bh ? po + e + 1 : pq + s + 1 + o, h, q);
             }

@@ -218,7 +218,9 @@ __global__ void __launch_bounds__(256) k_step_tma(StepArgs a, int32_t* err) {
                     st<S, Q>(D, a.stride, L::opp(q), n, f[q]);
                 } else {
                     const bool back = (missing >> L::opp(q)) & 1u;
-                    st_sel<S, Q>(D, (uint32_t)a.stride, q, nb_id(K, n0, lane, X::a(q), X::b(q), X::r(q)), back, n, f[q]);
+                    const bool keep = !back || bounce_back_pop<Q>(L::opp(q), (wmask >> lane) & 1u, a.corr);
+                    st_sel<S, Q>(D, (uint32_t)a.stride, q, nb_id(K, n0, lane, X::a(q), X::b(q), X::r(q)), back, n,
+                                 keep ? f[q] : init_work<S, Q>(q));
                 }
             }
         }
