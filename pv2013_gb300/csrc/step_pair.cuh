@@ -305,7 +305,7 @@ __global__ void __launch_bounds__(256) __maxnreg__((PairMaxReg<Q, S, MODE>::valu
     const uint32_t bm_all = act ? d1.x : 0u;
     const uint32_t zm_all = act ? d0.w : 0u;
     uint32_t m_lo = 0u, m_hi = 0u;
-    if ((bm_all >> (2 * t)) & 3u) {
+    if (MODE != MODE_AA_EVEN && ((bm_all >> (2 * t)) & 3u)) {
         const int32_t ms = (int32_t)d1.z + __popc(bm_all & ((1u << (2 * t)) - 1u));
         if ((bm_all >> (2 * t)) & 1u) m_lo = __ldg(a.mmask + ms);
         if ((bm_all >> (2 * t + 1)) & 1u) m_hi = __ldg(a.mmask + ms + ((bm_all >> (2 * t)) & 1u));
@@ -336,18 +336,20 @@ __global__ void __launch_bounds__(256) __maxnreg__((PairMaxReg<Q, S, MODE>::valu
     };
 
     W raw[Q];
-    __shared__ int32_t ksm[8][8][8];     // column bases of each warp's chunks
-    // the warp's shared words: the AA odd launch's bounce-back sources, then
-    // the Zou-He path's staging (one word per population and lane)
+    // dynamic shared memory: per warp one word per population and lane (the
+    // AA odd launch's bounce-back sources, then the Zou-He path's staging);
+    // after all warps' words, the AA odd launch's column bases (8 per piece,
+    // at most 8 pieces per warp)
     extern __shared__ __align__(16) unsigned char zsm[];
     W* buf = (W*)zsm + (threadIdx.x >> 5) * (Q * 32) + lane;
+    int32_t* ksm = reinterpret_cast<int32_t*>((W*)zsm + (blockDim.x >> 5) * (Q * 32)) + (threadIdx.x >> 5) * 64;
     if (act) {
         int32_t K[8];
         if constexpr (MODE != MODE_AA_EVEN) load_K(K, false);
         if constexpr (MODE == MODE_AA_ODD) {
             if (t == 0) {
 #pragma unroll
-                for (int c = 0; c < 8; ++c) ksm[threadIdx.x >> 5][pw][c] = K[c];
+                for (int c = 0; c < 8; ++c) ksm[pw * 8 + c] = K[c];
             }
             // boundary lanes: own words (slot q holds f*_opp(q) of the even
             // launch, the bounce-back value of population q), in flight with
@@ -394,7 +396,8 @@ __global__ void __launch_bounds__(256) __maxnreg__((PairMaxReg<Q, S, MODE>::valu
     if constexpr (MODE == MODE_AA_ODD) __syncwarp();
     // AA odd: missing populations (boundary nodes) take the bounced value from
     // the node's own word or the initial value (bounce_back_pop); only the
-    // populations missing somewhere in the warp are visited
+    // populations missing somewhere in the warp are visited (a per-lane loop
+    // over the missing bits through shared memory measured 6 % slower)
     if constexpr (MODE == MODE_AA_ODD) {
         // every lane that issued own-word copies waits for them here, before
         // the buffer is read or reused (a boundary node may miss no population)
@@ -488,7 +491,7 @@ __global__ void __launch_bounds__(256) __maxnreg__((PairMaxReg<Q, S, MODE>::valu
             asm volatile("ld.global.nc.u32 %0, [%1];" : "=r"(wm) : "l"(&cw[0].z));   // wmask
         vm = (vm >> (2 * t)) & 3u;
         wm = (wm >> (2 * t)) & 3u;
-        const volatile int32_t* ks = ksm[threadIdx.x >> 5][pw];
+        const volatile int32_t* ks = ksm + pw * 8;
         // whole-word stores of the directions without a run-axis component
         // only when no lane of the warp has a ghost slot or a bounce-back
         // (a warp-uniform branch; per-lane it diverged, measured 1.5 % slower)
@@ -526,7 +529,7 @@ static lbm_status launch_pair_one(const StepArgs& a, int wpb, cudaStream_t st) {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kDevs)
         return fail(LBM_ERR_CUDA, "paired step kernel: device %d not supported", dev);
-    const size_t smem = (size_t)wpb * Q * 32 * sizeof(typename PairWord<S>::W);
+    const size_t smem = (size_t)wpb * (Q * 32 * sizeof(typename PairWord<S>::W) + (MODE == MODE_AA_ODD ? 256 : 0));
     if (smem > 48 * 1024 && opted[dev] < (int)smem) {
         const cudaError_t e = cudaFuncSetAttribute(k_step2<Q, S, MODE, RA>,
                                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
