@@ -344,6 +344,15 @@ lbm_status lbm_sim_restart(lbm_sim* s, const char* path, void* stream);
  * LBM_ERR_DIVERGED when a value is non-finite or |mass/mass0 - 1| > rel_tol. */
 lbm_status lbm_sim_set_divergence_tolerance(lbm_sim* s, double rel_tol);
 
+/* Poll limit of the bounded waits in the TMA-staged step kernel (staging 0):
+ * a warp that tests a stage's mbarrier this many times (non-blocking tests)
+ * without the staged copies arriving stops, after draining its copies in flight, and the next
+ * monitor, fields or checkpoint call returns LBM_ERR_TIMEOUT (once; the
+ * state is then incomplete).  0 restores the default (2^22 polls).  The
+ * reference has no counterpart: its exchange errors print and continue
+ * (Simulation.cpp:237-239). */
+lbm_status lbm_sim_set_wait_limit(lbm_sim* s, uint32_t polls);
+
 void lbm_sim_destroy(lbm_sim* s);
 
 /* ------------------------------------------------------------------------ */

@@ -335,10 +335,13 @@ def ref_available(Q=19):
 
 def run_reference(stl_path, spacing, grid=None, preds=(), preset=None, tau=None, outlet_rho=None, steps=0,
                   profile=None, amp=None, inlet_dir=(0.0, -1.0, 0.0), Q=19, vtk_dir=None, workdir=None,
-                  flags_path=None, warmup=0):
+                  flags_path=None, warmup=0, wss=False):
     """Runs the reference harness; returns its outputs as numpy arrays.  With
     flags_path the node-type field of the (explicit) grid is read from that file
-    instead of the reference's voxelizer."""
+    instead of the reference's voxelizer.  With wss the reference's
+    ComputeVelocityGradientAtWall + ComputeWallShearStress run after the steps:
+    res["wss"] per wall node, res["wall_nodes"] their grid indices
+    (Simulation.cpp:1374-1421)."""
     wd = workdir or tempfile.mkdtemp(prefix="pv2013_ref_")
     os.makedirs(wd, exist_ok=True)
     lines = [f"stl {stl_path}", f"spacing {spacing!r}"]
@@ -370,6 +373,8 @@ def run_reference(stl_path, spacing, grid=None, preds=(), preset=None, tau=None,
         ap = os.path.join(wd, "amp.bin")
         np.asarray(amp, dtype=np.float64).tofile(ap)
         lines.append(f"amp_table {ap}")
+    if wss:
+        lines.append("wss 1")
     out = os.path.join(wd, "ref")
     lines.append(f"out {out}")
     run = os.path.join(wd, "run.txt")
@@ -396,4 +401,19 @@ def run_reference(stl_path, spacing, grid=None, preds=(), preset=None, tau=None,
         res["u"] = np.fromfile(out + ".u", dtype=np.float64).reshape(-1, 3)
         t = open(out + ".time").read().split()
         res["time"] = {"steps": int(t[0]), "nodes": int(t[1]), "seconds": float(t[2])}
+    if os.path.exists(out + ".wss"):
+        res["wss"] = np.fromfile(out + ".wss", dtype=np.float64)
+        res["wall_nodes"] = np.fromfile(out + ".wallnodes", dtype=np.int64)
     return res
+
+
+def reference_read_stl_binary(path, workdir=None):
+    """Triangles (n, 12) as the reference's Reader::readSTLBinary returns them
+    (GeometryReader.cpp:119-176: float vertices, normal renormalised in float)."""
+    wd = workdir or tempfile.mkdtemp(prefix="pv2013_ref_")
+    out = os.path.join(wd, "ref")
+    run = os.path.join(wd, "run.txt")
+    with open(run, "w") as fh:
+        fh.write(f"stl_binary {path}\nout {out}\n")
+    subprocess.run([REF_BIN[19], run], check=True, capture_output=True)
+    return np.fromfile(out + ".tris", dtype=np.float64).reshape(-1, 12)

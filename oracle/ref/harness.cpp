@@ -30,8 +30,16 @@
 //   flags <file>               node-type field (uint8, x-major, 1 = Fluid) of the box
 //                              grid, used instead of labelPoints (for timing the
 //                              step loop on a sample of a large geometry)
+//   wss 1                      after the steps, ComputeVelocityGradientAtWall and
+//                              ComputeWallShearStress (Simulation.cpp:1374-1421):
+//                              writes <prefix>.wss and <prefix>.wallnodes (grid
+//                              indices), in WallBoundaryNode_ order
+//   stl_binary <path>          only reads the binary STL with Reader::readSTLBinary
+//                              (GeometryReader.cpp:119-176) and writes <prefix>.tris
+//                              (12 doubles per triangle, Triangle's field order)
 //   out <prefix>               writes <prefix>.flags, .lists, .nodes, .f, .rho, .u
 #include "ComplexGeometry.h"
+#include "GeometryReader.h"
 #include "LatticeModel.h"
 #include "Simulation.h"
 #include "Subdomain.h"
@@ -84,7 +92,8 @@ int main(int argc, char** argv) {
     if (argc < 2) { std::fprintf(stderr, "usage: %s <run file>\n", argv[0]); return 2; }
     MPI_Init(&argc, &argv);
     std::ifstream run(argv[1]);
-    std::string line, stl, out = "ref", vtkdir, profile_path, amp_path, flags_path;
+    std::string line, stl, out = "ref", vtkdir, profile_path, amp_path, flags_path, stl_binary;
+    bool want_wss = false;
     double spacing = 1.0, tau = 0.8, box[3] = {0, 0, 0};
     int dims[3] = {0, 0, 0}, steps = 0, warmup = 0;
     bool have_box = false, preset = false;
@@ -116,6 +125,18 @@ int main(int argc, char** argv) {
         else if (key == "amp_table") ss >> amp_path;
         else if (key == "out") ss >> out;
         else if (key == "flags") ss >> flags_path;
+        else if (key == "wss") { int w = 0; ss >> w; want_wss = w != 0; }
+        else if (key == "stl_binary") ss >> stl_binary;
+    }
+    if (!stl_binary.empty()) {
+        Reader R;
+        const std::vector<Triangle> tris = R.readSTLBinary(stl_binary);
+        std::vector<double> v;
+        for (const Triangle& t : tris)
+            for (double x : {t.x1, t.y1, t.z1, t.x2, t.y2, t.z2, t.x3, t.y3, t.z3, t.nx, t.ny, t.nz}) v.push_back(x);
+        write_vec(out + ".tris", v);
+        MPI_Finalize();
+        return 0;
     }
 
     auto t0 = std::chrono::steady_clock::now();
@@ -257,6 +278,18 @@ int main(int argc, char** argv) {
     write_vec(out + ".rho", rho);
     write_vec(out + ".u", u);
     write_vec(out + ".nodes", nodes);
+    if (want_wss) {
+        sim.ComputeVelocityGradientAtWall();
+        sim.ComputeWallShearStress();
+        std::vector<double> wss;
+        std::vector<int64_t> wn;
+        for (auto& n : D.WallBoundaryNode_) {
+            wss.push_back(n->wall_shear_stress);
+            wn.push_back(((int64_t)n->x_position * Ny + n->y_position) * Nz + n->z_position);
+        }
+        write_vec(out + ".wss", wss);
+        write_vec(out + ".wallnodes", wn);
+    }
     MPI_Finalize();
     return 0;
 }

@@ -11,7 +11,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "_lib", "liblbm_gb300.so")
 
 LBM_OK = 0
-ERR_ARG, ERR_STATE = 7, 8
+ERR_TIMEOUT, ERR_ARG, ERR_STATE = 6, 7, 8
 STATUS_NAMES = {
     0: "LBM_OK", 1: "LBM_ERR_IO", 2: "LBM_ERR_PARSE", 3: "LBM_ERR_NOMEM", 4: "LBM_ERR_CUDA",
     5: "LBM_ERR_DIVERGED", 6: "LBM_ERR_TIMEOUT", 7: "LBM_ERR_ARG", 8: "LBM_ERR_STATE", 9: "LBM_ERR_NODEV",
@@ -138,6 +138,7 @@ PROTOTYPES = {
     "lbm_sim_instance_offsets": (C.c_int, [C.c_void_p, C.c_void_p, C.c_size_t]),
     "lbm_sim_monitors": (C.c_int, [C.c_void_p, _P(Monitors), C.c_void_p]),
     "lbm_sim_set_divergence_tolerance": (C.c_int, [C.c_void_p, C.c_double]),
+    "lbm_sim_set_wait_limit": (C.c_int, [C.c_void_p, C.c_uint32]),
     "lbm_sim_destroy": (None, [C.c_void_p]),
     "lbm_synth_cylinder": (C.c_int, [C.c_double, C.c_double, C.c_int32, C.c_int32, _P(C.c_double),
                                      _P(_P(Tri)), _P(C.c_size_t)]),

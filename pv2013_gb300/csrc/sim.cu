@@ -540,6 +540,7 @@ struct lbm_sim {
     int64_t part_blocks = 0;
     double mass0 = 0.0;
     double div_tol = 1e-2;
+    uint32_t spin_limit = 0;       // TMA-staged kernel's wait limit (0 = its default)
     // wall nodes: output positions in wall-list order (built on first use)
     int64_t* wall_pos = nullptr;
     int64_t nwall = -1;
@@ -789,6 +790,7 @@ lbm_status sim_launch(lbm_sim* S, int mode, bool dry, void* src, void* dst, int6
     a.out_f = of; a.out_rho = orho; a.out_u = ou; a.out_pos = S->out_pos; a.n_nodes = S->NF;
     a.mmask = S->mmask;
     a.corr = S->corr;
+    a.spin_limit = S->spin_limit;
     a.piece_lg = S->piece == 8 ? 2 : (S->piece == 16 ? 3 : 4);
     if (!dry && S->npl == 2) {
         a.chunks = S->chunks2;
@@ -875,12 +877,18 @@ lbm_status sim_dry(lbm_sim* S, double* of, double* orho, double* ou, bool partia
     return LBM_OK;
 }
 
-// Reads the step kernel's error flag (synchronises the stream).
+// Reads the step kernel's error flag (synchronises the stream) and clears it:
+// a timeout is reported once.
 lbm_status check_timeout(lbm_sim* S, cudaStream_t st) {
     int32_t e = 0;
     LBM_CUDA(cudaMemcpyAsync(&e, S->err, sizeof e, cudaMemcpyDeviceToHost, st));
     LBM_CUDA(cudaStreamSynchronize(st));
-    if (e) return fail(LBM_ERR_TIMEOUT, "a bounded wait in the step kernel gave up (staged copies did not arrive)");
+    if (e) {
+        LBM_CUDA(cudaMemsetAsync(S->err, 0, sizeof(int32_t), st));
+        LBM_CUDA(cudaStreamSynchronize(st));
+        return fail(LBM_ERR_TIMEOUT, "a bounded wait in the step kernel gave up (staged copies did not arrive)%s; "
+                    "the populations are incomplete", (e & 2) ? ", and draining its copies in flight gave up too" : "");
+    }
     return LBM_OK;
 }
 
@@ -1477,6 +1485,13 @@ lbm_status lbm_sim_monitors(lbm_sim* S, lbm_monitors* out, void* stream) {
     if (!S || !out) return fail(LBM_ERR_ARG, "lbm_sim_monitors: null argument");
     clear_error();
     return sim_monitors(S, out, (cudaStream_t)stream);
+}
+
+lbm_status lbm_sim_set_wait_limit(lbm_sim* S, uint32_t polls) {
+    if (!S) return fail(LBM_ERR_ARG, "lbm_sim_set_wait_limit: null handle");
+    S->spin_limit = polls;
+    free_graph(S);                         // captured launches carry the old limit
+    return LBM_OK;
 }
 
 lbm_status lbm_sim_set_divergence_tolerance(lbm_sim* S, double rel_tol) {

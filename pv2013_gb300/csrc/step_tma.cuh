@@ -16,8 +16,12 @@
 //
 // Arithmetic, boundary handling and the streaming patterns are those of
 // k_step (shared device functions); only the source of the gathered values
-// changes.  Waits on an mbarrier are bounded: after kSpinLimit polls the warp
-// records an error (read back by the host as LBM_ERR_TIMEOUT) and stops.
+// changes.  Waits on an mbarrier are bounded: after kSpinLimit polls (or
+// a.spin_limit non-blocking tests, when set) the warp records an error (bit 0 of *err, read back by
+// the host as LBM_ERR_TIMEOUT), drains the stages still in flight with waits
+// bounded by kSpinLimit each, and stops.  A drain that gives up too sets bit 1:
+// that only follows a stall of the copy hardware itself, and the warp may then
+// exit with bulk copies still writing into its shared memory.
 #pragma once
 #include "step_kernel.cuh"
 
@@ -61,6 +65,19 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t bar, uint32_t parity) {
     asm volatile(
         "{\n\t.reg .pred p;\n\t"
         "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// non-blocking test of a phase (try_wait may suspend the thread for a while)
+__device__ __forceinline__ bool mbar_test_wait(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
         "selp.u32 %0, 1, 0, p;\n\t}"
         : "=r"(ok)
         : "r"(bar), "r"(parity)
@@ -156,19 +173,25 @@ __global__ void __launch_bounds__(256) k_step_tma(StepArgs a, int32_t* err) {
             const uint32_t ph = (parity >> s) & 1u;
             uint32_t spins = 0;
             bool ok = true;
-            while (!mbar_try_wait(bar, ph)) {
-                if (++spins > kSpinLimit) { ok = false; break; }
+            if (a.spin_limit) {
+                while (!mbar_test_wait(bar, ph))
+                    if (++spins >= a.spin_limit) { ok = false; break; }
+            } else {
+                while (!mbar_try_wait(bar, ph))
+                    if (++spins >= kSpinLimit) { ok = false; break; }
             }
             if (!ok) {
                 // record the failure, then drain (bounded) every stage still in flight
-                if (lane == 0) atomicOr(err, 1);
+                bool drained = true;
                 for (int64_t j = k; j < k + kStages && chunk_of(j) < a.nchunks; ++j) {
                     const int sj = (int)(j % kStages);
                     const uint32_t bj = smem_addr(ring + sj * LY::BYTES + LY::BAR);
-                    for (uint32_t t = 0; t < kSpinLimit && !mbar_try_wait(bj, (parity >> sj) & 1u); ++t) {
-                    }
+                    uint32_t t = 0;
+                    while (!mbar_try_wait(bj, (parity >> sj) & 1u))
+                        if (++t >= kSpinLimit) { drained = false; break; }
                     parity ^= 1u << sj;
                 }
+                if (lane == 0) atomicOr(err, drained ? 1 : 3);
                 return;
             }
             parity ^= 1u << s;

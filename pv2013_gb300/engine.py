@@ -401,6 +401,10 @@ class Simulation:
     def set_divergence_tolerance(self, tol):
         check(load().lbm_sim_set_divergence_tolerance(self._h, float(tol)))
 
+    def set_wait_limit(self, polls):
+        """Poll limit of the TMA-staged kernel's bounded waits (0 = default)."""
+        check(load().lbm_sim_set_wait_limit(self._h, int(polls)))
+
     def wall_shear_stress(self):
         """Wall shear stress at every wall node, wall-list order (ComputeWallShearStress)."""
         lib = load()

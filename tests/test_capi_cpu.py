@@ -117,7 +117,7 @@ def test_binary_stl_reader(tmp_path):
     assert np.array_equal(got[:, :9], tris[:, :9].astype(np.float64))
     n = tris[:, 9:12]
     norm = np.sqrt((n[:, 0] * n[:, 0] + n[:, 1] * n[:, 1]) + n[:, 2] * n[:, 2]).astype(np.float32)
-    assert np.allclose(got[:, 9:12], (n / norm[:, None]).astype(np.float64), rtol=0, atol=1e-7)
+    assert np.array_equal(got[:, 9:12], (n / norm[:, None]).astype(np.float64))   # float arithmetic, exact
 
 
 def _open_edges(t):

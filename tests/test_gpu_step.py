@@ -218,3 +218,31 @@ def test_corrections_act_on_boundary_nodes_first():
     assert d.max() > 0
     bnd = set(geom.list(_capi.LIST_BOUNDARY).tolist())
     assert int(a.nodes()[np.argmax(d)]) in bnd
+
+
+def test_bounded_wait_runs_out_and_the_handle_recovers(tmp_path):
+    """The TMA-staged kernel's mbarrier waits are bounded: with a limit of one
+    non-blocking test the staged copies cannot have arrived, the warps record
+    the give-up and drain their copies, the next monitor call reports
+    LBM_ERR_TIMEOUT once; with the default limit restored and the state
+    restored from a checkpoint the run continues bit for bit."""
+    c = cases.pipe()
+    geom = c.geometry()
+    specs = c.boundary_specs(geom)
+    ref = Simulation(geom, c.tau, specs, precision="f64", pattern="pull", staging=0)
+    sim = Simulation(geom, c.tau, specs, precision="f64", pattern="pull", staging=0)
+    ref.step(4)
+    sim.step(4)
+    path = str(tmp_path / "w.ckpt")
+    sim.checkpoint(path)
+    sim.set_wait_limit(1)
+    sim.step(2)
+    with pytest.raises(_capi.LbmError) as e:
+        sim.monitors()
+    assert e.value.status == _capi.ERR_TIMEOUT
+    sim.monitors()          # reported once: this call succeeds
+    sim.set_wait_limit(0)
+    sim.restart(path)
+    sim.step(6)
+    ref.step(6)
+    assert np.array_equal(sim.fields()[0], ref.fields()[0])

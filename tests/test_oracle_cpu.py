@@ -56,7 +56,7 @@ ref19 = pytest.mark.skipif(not os.path.exists(os.path.join(os.path.dirname(__fil
                                                             "pv2013_ref")), reason="reference checker not built")
 
 
-def _ref_case(O, case, steps, tmp):
+def _ref_case(O, case, steps, tmp, wss=False):
     stl = os.path.join(tmp, "case.stl")
     Reader.writeSTLASCII(stl, case.triangles)
     geo = O.geometry(case.triangles, case.spacing, case.grid, case.predicates)
@@ -67,7 +67,8 @@ def _ref_case(O, case, steps, tmp):
     prof = np.maximum(0, 1 - ((i - cx) ** 2 + (k - cz) ** 2) / case.inlet.radius ** 2)
     amp = case.amp_table()
     ref = O.run_reference(stl, case.spacing, grid=case.grid, preds=O.predicate_tuples(case.predicates),
-                          tau=case.tau, outlet_rho=case.outlet_rho, steps=steps, profile=prof, amp=amp, workdir=tmp)
+                          tau=case.tau, outlet_rho=case.outlet_rho, steps=steps, profile=prof, amp=amp, workdir=tmp,
+                          wss=wss)
     return geo, prof, amp, ref
 
 
@@ -244,3 +245,45 @@ def test_face_kinds_are_covariant_under_axis_maps(oracle_mod, Q):
                 g1 = np.flip(g1, axis=a)
         ids0 = g1.reshape(-1)[role1 >= 0]          # old node id of every new node, new order
         assert np.abs(f1[:, dmap] - f0[ids0]).max() < 1e-14, (perm, flip)
+
+
+@ref19
+@pytest.mark.parametrize("make,steps", [(cases.pipe, 20), (lambda: cases.vessel(4006, h=3.0), 12)])
+def test_oracle_wss_equals_reference(oracle_mod, make, steps):
+    """Wall shear stress: the restatement equals the reference's
+    ComputeVelocityGradientAtWall + ComputeWallShearStress
+    (Simulation.cpp:1374-1421) bit for bit, on the wall nodes in the
+    reference's order, after the reference's own steps."""
+    O = oracle_mod
+    c = make()
+    if hasattr(c.inlet, "period") and c.inlet.period > 0:
+        c.inlet.period = 7
+    with tempfile.TemporaryDirectory() as tmp:
+        geo, prof, amp, ref = _ref_case(O, c, steps, tmp, wss=True)
+    sim = O.run_case(19, geo, c.tau, {0: (O.BC_VEL_NEGY, 1.0), 2: (O.BC_PRESS_POSY, c.outlet_rho)}, steps,
+                     profile=prof, amp=amp)
+    assert np.array_equal(ref["wall_nodes"], geo["lists"]["wall"])
+    w = sim.wss()
+    assert len(w) == len(ref["wss"]) and np.any(w > 0)
+    assert np.array_equal(w, ref["wss"])
+
+
+@ref19
+def test_binary_stl_reader_equals_reference(oracle_mod, tmp_path):
+    """lbm_stl_read_binary returns the reference's Reader::readSTLBinary
+    triangles bit for bit (float vertices; the file's normal renormalised in
+    float, GeometryReader.cpp:119-176), on facets with unnormalised normals."""
+    from pv2013_gb300 import Reader
+    rng = np.random.default_rng(11)
+    tris = cases.vessel(4001, h=3.0).triangles.astype(np.float32)
+    tris[:, 9:12] *= rng.uniform(0.2, 7.0, size=(len(tris), 1)).astype(np.float32)
+    p = tmp_path / "b.stl"
+    with open(p, "wb") as fh:
+        fh.write(b"solid binary" + b"\0" * 68)
+        fh.write(np.uint32(len(tris)).tobytes())
+        for t in tris:
+            fh.write(t[9:12].tobytes() + t[0:9].tobytes() + b"\0\0")
+    mine = Reader.readSTLBinary(str(p))
+    ref = oracle_mod.reference_read_stl_binary(str(p), workdir=str(tmp_path))
+    assert mine.shape == ref.shape == (len(tris), 12)
+    assert np.array_equal(mine, ref)
