@@ -363,7 +363,8 @@ def gpu_arm(args, rank, world):
         enf = sum(g.info.n_fluid for g in egeo)
         esim = Simulation(egeo, [c.tau for c in ens], [c.boundary_specs(g) for c, g in zip(ens, egeo)],
                           precision="f16s", pattern=args.pattern, piece_slots=args.piece_slots)
-        esim.autotune(launches=10)
+        esim.step(1)                         # after an even launch both patterns are candidates
+        tuned = esim.autotune(launches=10)
         esec = max_over_ranks(time_steps(esim, args.batch_steps, args.warmup, torch), world, "cuda")
         einfo = esim.info()
         batched = {"workload": "ensemble of 64 tortuous vessels (seeds 4000-4063), per-instance tau, inlet amplitude "
@@ -371,7 +372,9 @@ def gpu_arm(args, rank, world):
                    "fluid_nodes": enf, "steps": args.batch_steps, "mlups": enf * args.batch_steps / esec / 1e6 * world,
                    "ms_per_step": esec / args.batch_steps * 1e3,
                    "kernel": {"nodes_per_lane": einfo.nodes_per_lane, "piece_slots": einfo.piece_slots,
-                              "warps_per_block": einfo.warps_per_block}}
+                              "warps_per_block": einfo.warps_per_block,
+                              "pattern": {0: "pull", 1: "aa"}[einfo.pattern],
+                              "candidates": len(tuned)}}
         del esim, egeo
 
     # --- roofline of the step kernel ------------------------------------------

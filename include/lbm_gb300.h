@@ -290,13 +290,20 @@ lbm_status lbm_sim_info_get(const lbm_sim* s, lbm_sim_info* info);
 
 /* Autotuner: times every step-kernel variant the handle can run -- one node
  * per lane with direct loads or TMA staging, two nodes per lane (FP32 and
- * 16-bit storage), each with 1, 2, 4 and 8 warps per block -- for `launches`
- * launches on a scratch copy of the state (the simulation does not advance),
- * and keeps the fastest for later steps.  entries (may be NULL) receives up
- * to cap results, *n (may be NULL) their number.  Needs device memory for one
- * more copy of the populations (LBM_ERR_NOMEM otherwise, nothing changed). */
+ * 16-bit storage) with 8-, 16- and 32-slot pieces, each with 1, 2, 4 and 8
+ * warps per block, in the current streaming pattern and in the other one
+ * where the state converts now (lbm_sim_set_pattern) and its memory fits --
+ * for `launches` launches on scratch copies of the state (the simulation does
+ * not advance), and keeps the fastest for later steps (converting the state
+ * when the pattern changes; results are unchanged).  The layout (structure
+ * of arrays) is not a candidate: a blocked layout measured 6 % slower.
+ * entries (may be NULL) receives up to cap results, *n (may be NULL) their
+ * number.  Needs device memory for one or two more copies of the populations
+ * (LBM_ERR_NOMEM otherwise, nothing changed). */
 typedef struct lbm_tune_entry {
     int32_t nodes_per_lane, staging, warps_per_block, chosen;
+    int32_t pattern;           /* lbm_pattern of the candidate */
+    int32_t piece_slots;       /* two nodes per lane: node slots per piece, else 0 */
     double ms_per_launch;
 } lbm_tune_entry;
 lbm_status lbm_sim_autotune(lbm_sim* s, int32_t launches, void* stream, lbm_tune_entry* entries, size_t cap,
@@ -352,6 +359,23 @@ lbm_status lbm_sim_set_divergence_tolerance(lbm_sim* s, double rel_tol);
  * reference has no counterpart: its exchange errors print and continue
  * (Simulation.cpp:237-239). */
 lbm_status lbm_sim_set_wait_limit(lbm_sim* s, uint32_t polls);
+
+/* Failure-test hook (no counterpart in the reference): while enabled, the
+ * TMA-staged step kernel leaves each warp's first stage unissued, so that
+ * stage's bounded wait runs out (no copy is in flight on it) and the next
+ * monitor, fields or checkpoint call reports LBM_ERR_TIMEOUT.  The state of
+ * such a step is incomplete; restore it (lbm_sim_restart) after disabling. */
+lbm_status lbm_sim_test_stall(lbm_sim* s, int32_t enable);
+
+/* Converts the state to another streaming pattern (LBM_PULL or LBM_AA); the
+ * run continues with the same results.  After an AA even (node-local)
+ * launch the AA state is the pull state with its population planes
+ * permuted, so AA -> pull needs that state (an odd number of steps done
+ * since the AA run started; LBM_ERR_STATE otherwise) and memory for the
+ * second lattice; pull -> AA always works and frees one lattice.  No
+ * counterpart in the reference, which has one streaming scheme
+ * (Simulation.cpp:184-198). */
+lbm_status lbm_sim_set_pattern(lbm_sim* s, int32_t pattern, void* stream);
 
 void lbm_sim_destroy(lbm_sim* s);
 

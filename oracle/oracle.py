@@ -407,6 +407,18 @@ def run_reference(stl_path, spacing, grid=None, preds=(), preset=None, tau=None,
     return res
 
 
+def reference_pulsatile(n, workdir=None):
+    """The reference's inlet waveform (pulsatile.h:8-31, selected as in
+    Simulation.cpp:875-900) at x = 0.9 s * s / n, s = 0..n-1."""
+    wd = workdir or tempfile.mkdtemp(prefix="pv2013_ref_")
+    out = os.path.join(wd, "ref")
+    run = os.path.join(wd, "run.txt")
+    with open(run, "w") as fh:
+        fh.write(f"pulsatile {int(n)}\nout {out}\n")
+    subprocess.run([REF_BIN[19], run], check=True, capture_output=True)
+    return np.fromfile(out + ".pulsatile", dtype=np.float64)
+
+
 def reference_read_stl_binary(path, workdir=None):
     """Triangles (n, 12) as the reference's Reader::readSTLBinary returns them
     (GeometryReader.cpp:119-176: float vertices, normal renormalised in float)."""

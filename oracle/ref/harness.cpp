@@ -37,12 +37,17 @@
 //   stl_binary <path>          only reads the binary STL with Reader::readSTLBinary
 //                              (GeometryReader.cpp:119-176) and writes <prefix>.tris
 //                              (12 doubles per triangle, Triangle's field order)
+//   pulsatile <n>              only evaluates the reference's inlet waveform (the
+//                              Pulsatile polynomials of pulsatile.h, selected as in
+//                              Simulation::getInletVelocity, Simulation.cpp:875-900)
+//                              at x = 0.9 s / n ... and writes <prefix>.pulsatile
 //   out <prefix>               writes <prefix>.flags, .lists, .nodes, .f, .rho, .u
 #include "ComplexGeometry.h"
 #include "GeometryReader.h"
 #include "LatticeModel.h"
 #include "Simulation.h"
 #include "Subdomain.h"
+#include "pulsatile.h"
 
 #include <chrono>
 #include <cstdio>
@@ -94,6 +99,7 @@ int main(int argc, char** argv) {
     std::ifstream run(argv[1]);
     std::string line, stl, out = "ref", vtkdir, profile_path, amp_path, flags_path, stl_binary;
     bool want_wss = false;
+    int pulsatile_n = 0;
     double spacing = 1.0, tau = 0.8, box[3] = {0, 0, 0};
     int dims[3] = {0, 0, 0}, steps = 0, warmup = 0;
     bool have_box = false, preset = false;
@@ -127,6 +133,23 @@ int main(int argc, char** argv) {
         else if (key == "flags") ss >> flags_path;
         else if (key == "wss") { int w = 0; ss >> w; want_wss = w != 0; }
         else if (key == "stl_binary") ss >> stl_binary;
+        else if (key == "pulsatile") ss >> pulsatile_n;
+    }
+    if (pulsatile_n > 0) {
+        Pulsatile P;
+        std::vector<double> v;
+        for (int s = 0; s < pulsatile_n; ++s) {
+            const double x = P.period * s / pulsatile_n;
+            const double nx = std::fmod(x, P.period);
+            double vel = 0.0;
+            if (nx >= 0 && nx < 0.1 * P.period) vel = P.InletVelequation1(nx);
+            else if (nx >= 0.1 * P.period && nx < 0.3 * P.period) vel = P.InletVelequation2(nx);
+            else if (nx >= 0.3 * P.period && nx < 0.9 * P.period) vel = P.InletVelequation3(nx);
+            v.push_back(vel);
+        }
+        write_vec(out + ".pulsatile", v);
+        MPI_Finalize();
+        return 0;
     }
     if (!stl_binary.empty()) {
         Reader R;

@@ -6,12 +6,14 @@
 
 The run file uses the reference's ConfigReader format (ConfigReader.cpp:13-51):
 one `key value` pair per line, `#` starts a comment line; command-line options
-override it.  Keys: case, stl, preset, spacing, tau, steps, warmup, precision,
-pattern, Q, u_in, outlet_rho, run_axis, staging, warps_per_block, nodes_per_lane,
-piece_slots.
+override it.  Keys: case, stl, preset, spacing, box, tau, steps, warmup,
+precision, pattern, Q, u_in, outlet_rho, run_axis, staging, warps_per_block,
+nodes_per_lane, piece_slots.  `boundary <list> ... end` blocks give each
+inlet/outlet list its plane predicate and boundary condition (runfile.py).
 
 Named cases are the seeded synthetic workloads of pv2013_gb300.cases (pipe,
-pipe_x, bifurcation, vascular_tree, vessel); `--stl FILE --preset pv2013` runs
+pipe_x, bifurcation, vascular_tree, vessel); `--stl FILE` with boundary blocks
+runs any surface (ASCII or binary STL); `--stl FILE --preset pv2013` runs
 an STL with the PV2013 inlet/outlet planes (ComplexGeometry.cpp:579-638), the
 reference's uniform inlet velocity (0, -u_in, 0) (Boundary.cpp:9, Input.h:7)
 and its outlet density 1.01 (Simulation.cpp:954).
@@ -24,33 +26,39 @@ import json
 import sys
 import time
 
-KEYS = {"case": str, "stl": str, "preset": str, "spacing": float, "tau": float, "steps": int, "warmup": int,
-        "precision": str, "pattern": str, "Q": int, "u_in": float, "outlet_rho": float, "run_axis": int,
-        "staging": int, "warps_per_block": int, "nodes_per_lane": int, "piece_slots": int, "h": float}
+from . import runfile
+from .runfile import KEYS
 
 
 def read_run_file(path):
-    """key/value pairs of a ConfigReader-format file; values converted by key."""
-    out = {}
-    with open(path) as fh:
-        for n, line in enumerate(fh, 1):
-            line = line.rstrip("\n")
-            if not line or line[0] == "#":
-                continue
-            parts = line.split(None, 1)
-            if len(parts) != 2:
-                raise ValueError(f"{path}:{n}: expected 'key value'")
-            k, v = parts[0], parts[1].strip()
-            if k not in KEYS:
-                raise ValueError(f"{path}:{n}: unknown key {k!r}")
-            out[k] = KEYS[k](v)
-    return out
+    """key/value pairs of a ConfigReader-format file (boundary blocks aside)."""
+    return runfile.read(path)[0]
 
 
-def build_problem(cfg):
+def read_surface(path):
+    """Triangles of an ASCII or binary STL (binary when it does not start with 'solid')."""
+    from .engine import Reader
+    with open(path, "rb") as fh:
+        head = fh.read(5)
+    return Reader.readSTLASCII(path) if head == b"solid" else Reader.readSTLBinary(path)
+
+
+def build_problem(cfg, blocks=()):
     """(geometry, tau, boundary specs, Q) for the configuration."""
     from . import _capi, cases
     from .engine import BoundarySpec, Geometry, Reader, pv2013_predicates
+    if blocks:
+        if cfg.get("stl"):
+            tris = read_surface(cfg["stl"])
+            grid = runfile.grid_of(cfg)
+            tau = cfg.get("tau", 0.8)
+        else:
+            case = cases.pipe() if cfg.get("case", "pipe") == "pipe" else None
+            if case is None:
+                raise ValueError("boundary blocks need an STL (or the pipe case)")
+            tris, grid, tau = case.triangles, runfile.grid_of(cfg) or case.grid, cfg.get("tau", case.tau)
+        g = Geometry(tris, cfg.get("spacing", 1.0), grid=grid, predicates=runfile.predicates(blocks))
+        return g, tau, runfile.boundary_specs(blocks, g), cfg.get("Q", 19)
     if cfg.get("stl"):
         if cfg.get("preset", "pv2013") != "pv2013":
             raise ValueError("an STL run needs --preset pv2013 (the only built-in predicate set)")
@@ -87,14 +95,14 @@ def main(argv=None):
     for k, t in KEYS.items():
         ap.add_argument("--" + k, type=t)
     a = ap.parse_args(argv)
-    cfg = read_run_file(a.run_file) if a.run_file else {}
+    cfg, blocks = runfile.read(a.run_file) if a.run_file else ({}, [])
     cfg.update({k: v for k, v in vars(a).items() if k in KEYS and v is not None})
 
     import torch
     from .engine import Simulation
     torch.cuda.init()
     t0 = time.time()
-    g, tau, specs, Q = build_problem(cfg)
+    g, tau, specs, Q = build_problem(cfg, blocks)
     t_geom = time.time() - t0
     t0 = time.time()
     sim = Simulation(g, tau, specs, Q=Q, precision=cfg.get("precision", "f64"), pattern=cfg.get("pattern", "pull"),

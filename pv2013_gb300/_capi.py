@@ -76,7 +76,8 @@ class SimParams(C.Structure):
 
 class TuneEntry(C.Structure):
     _fields_ = [("nodes_per_lane", C.c_int32), ("staging", C.c_int32), ("warps_per_block", C.c_int32),
-                ("chosen", C.c_int32), ("ms_per_launch", C.c_double)]
+                ("chosen", C.c_int32), ("pattern", C.c_int32), ("piece_slots", C.c_int32),
+                ("ms_per_launch", C.c_double)]
 
 
 class VtuArray(C.Structure):
@@ -139,6 +140,8 @@ PROTOTYPES = {
     "lbm_sim_monitors": (C.c_int, [C.c_void_p, _P(Monitors), C.c_void_p]),
     "lbm_sim_set_divergence_tolerance": (C.c_int, [C.c_void_p, C.c_double]),
     "lbm_sim_set_wait_limit": (C.c_int, [C.c_void_p, C.c_uint32]),
+    "lbm_sim_test_stall": (C.c_int, [C.c_void_p, C.c_int32]),
+    "lbm_sim_set_pattern": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
     "lbm_sim_destroy": (None, [C.c_void_p]),
     "lbm_synth_cylinder": (C.c_int, [C.c_double, C.c_double, C.c_int32, C.c_int32, _P(C.c_double),
                                      _P(_P(Tri)), _P(C.c_size_t)]),

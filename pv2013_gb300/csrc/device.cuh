@@ -159,6 +159,7 @@ struct StepArgs {
     int32_t piece_lg;         // paired kernel: log2 of the lanes per chunk piece (2, 3 or 4)
     int64_t pf_ahead;         // paired kernel: L2 prefetch distance in chunk pieces (0 = none)
     uint32_t spin_limit;      // TMA-staged kernel: polls of a stage's mbarrier before giving up (0 = default)
+    int32_t stall_first;      // TMA-staged kernel, failure tests: each warp's first stage is never issued
 };
 
 }  // namespace lbm

@@ -515,8 +515,11 @@ struct lbm_sim {
     void* buf[2] = {nullptr, nullptr};
     int cur = 0;                   // pull: buffer holding the current state
     Chunk* chunks = nullptr;
-    Chunk* chunks2 = nullptr;      // paired chunk table (nodes_per_lane = 2)
+    Chunk* chunks2 = nullptr;      // paired chunk table in use (nodes_per_lane = 2): chunks2s[piece]
     int64_t nchunks2 = 0;
+    Chunk* chunks2s[3] = {nullptr, nullptr, nullptr};   // paired tables of 8-, 16- and 32-slot pieces
+    int64_t nchunks2s[3] = {0, 0, 0};
+    int aa_phase = 0;              // AA: launch n is an even (node-local) launch when n + aa_phase is even
     ZSlot* zslots = nullptr;
     ListParam* lists = nullptr;
     InstParam* insts = nullptr;
@@ -541,6 +544,7 @@ struct lbm_sim {
     double mass0 = 0.0;
     double div_tol = 1e-2;
     uint32_t spin_limit = 0;       // TMA-staged kernel's wait limit (0 = its default)
+    int32_t stall_first = 0;       // failure tests: the TMA-staged kernel's first stages are not issued
     // wall nodes: output positions in wall-list order (built on first use)
     int64_t* wall_pos = nullptr;
     int64_t nwall = -1;
@@ -556,8 +560,8 @@ struct InstBuild {
     DBuf<int32_t> out_pos;         // output position of each node (-1 for ghosts)
     DBuf<Chunk> chunks;
     int64_t nchunks = 0;
-    DBuf<Chunk> chunks2;
-    int64_t nchunks2 = 0;
+    DBuf<Chunk> chunks2[3];        // paired pieces of 8, 16 and 32 slots
+    int64_t nchunks2[3] = {0, 0, 0};
     DBuf<uint32_t> mmask;
     int64_t nmask = 0;
     std::vector<ZSlot> zslots;
@@ -758,20 +762,24 @@ lbm_status build_instance(const lbm_geometry* g, const lbm_sim_params* p, int Q,
     k_col_fill<<<blocks_for(ncol, 128), 128, 0, st>>>(fa);
     LBM_CUDA(cudaGetLastError());
     if (npl == 2) {
-        // paired chunks share the missing masks (same boundary-node order)
-        DBuf<int64_t> coff2;
-        LBM_TRY(coff2.alloc(ncol, "paired chunk offsets"));
-        k_col_count2<<<blocks_for(ncol, 128), 128, 0, st>>>(type.p, D, piece, ccount.p);
-        LBM_TRY(scan::exclusive_scan(ccount.p, ncol, coff2.p, &out.nchunks2, st));
-        LBM_TRY(out.chunks2.alloc(out.nchunks2, "paired chunks"));
-        FillArgs f2 = fa;
-        f2.chunk_off = coff2.p;
-        f2.chunks = out.chunks2.p;
-        f2.mmask = nullptr;
-        f2.piece = piece;
-        k_col_fill2<<<blocks_for(ncol, 128), 128, 0, st>>>(f2);
-        LBM_CUDA(cudaGetLastError());
-        LBM_CUDA(cudaStreamSynchronize(st));   // coff2 is freed on return
+        // paired chunks of every piece size (the autotuner may switch sizes);
+        // they share the missing masks (same boundary-node order)
+        for (int k = 0; k < 3; ++k) {
+            const int pc = 8 << k;
+            DBuf<int64_t> coff2;
+            LBM_TRY(coff2.alloc(ncol, "paired chunk offsets"));
+            k_col_count2<<<blocks_for(ncol, 128), 128, 0, st>>>(type.p, D, pc, ccount.p);
+            LBM_TRY(scan::exclusive_scan(ccount.p, ncol, coff2.p, &out.nchunks2[k], st));
+            LBM_TRY(out.chunks2[k].alloc(out.nchunks2[k], "paired chunks"));
+            FillArgs f2 = fa;
+            f2.chunk_off = coff2.p;
+            f2.chunks = out.chunks2[k].p;
+            f2.mmask = nullptr;
+            f2.piece = pc;
+            k_col_fill2<<<blocks_for(ncol, 128), 128, 0, st>>>(f2);
+            LBM_CUDA(cudaGetLastError());
+            LBM_CUDA(cudaStreamSynchronize(st));   // coff2 is freed on return
+        }
     }
     int32_t herr = 0;
     LBM_CUDA(cudaMemcpyAsync(&herr, d_err, sizeof herr, cudaMemcpyDeviceToHost, st));
@@ -791,6 +799,7 @@ lbm_status sim_launch(lbm_sim* S, int mode, bool dry, void* src, void* dst, int6
     a.mmask = S->mmask;
     a.corr = S->corr;
     a.spin_limit = S->spin_limit;
+    a.stall_first = S->stall_first;
     a.piece_lg = S->piece == 8 ? 2 : (S->piece == 16 ? 3 : 4);
     if (!dry && S->npl == 2) {
         a.chunks = S->chunks2;
@@ -841,6 +850,19 @@ static lbm_status pair_first_launch(lbm_sim* S, cudaStream_t st) {
     return LBM_OK;
 }
 
+// The paired piece table of `piece` slots (8, 16 or 32) becomes the one in use.
+void select_piece(lbm_sim* S, int piece) {
+    const int k = piece == 8 ? 0 : (piece == 16 ? 1 : 2);
+    S->piece = piece;
+    S->chunks2 = S->chunks2s[k];
+    S->nchunks2 = S->nchunks2s[k];
+}
+
+// AA pattern: the launch at the current state is the even (node-local) one
+// when steps_done + aa_phase is even (aa_phase changes when a pull state
+// becomes an AA state, lbm_sim_set_pattern).
+int aa_mode(const lbm_sim* S) { return ((S->steps_done + S->aa_phase) & 1) == 0 ? MODE_AA_EVEN : MODE_AA_ODD; }
+
 // Launches one step at the current state; advances cur/steps_done.
 lbm_status sim_one_step(lbm_sim* S, int64_t step_arg, const int64_t* step_base, cudaStream_t st, bool advance_count) {
     Partials np = {nullptr, nullptr, nullptr, nullptr, nullptr};
@@ -850,8 +872,8 @@ lbm_status sim_one_step(lbm_sim* S, int64_t step_arg, const int64_t* step_base, 
                        nullptr, nullptr, st);
         S->cur = 1 - S->cur;
     } else {
-        const int mode = ((S->steps_done & 1) == 0) ? MODE_AA_EVEN : MODE_AA_ODD;
-        s = sim_launch(S, mode, false, S->buf[0], S->buf[0], step_arg, step_base, np, nullptr, nullptr, nullptr, st);
+        s = sim_launch(S, aa_mode(S), false, S->buf[0], S->buf[0], step_arg, step_base, np, nullptr, nullptr, nullptr,
+                       st);
     }
     if (advance_count) S->steps_done++;
     return s;
@@ -870,7 +892,7 @@ lbm_status sim_dry(lbm_sim* S, double* of, double* orho, double* ou, bool partia
     int mode;
     void* src;
     if (S->pattern == LBM_PULL) { mode = MODE_PULL; src = S->buf[S->cur]; }
-    else { mode = ((S->steps_done & 1) == 0) ? MODE_AA_EVEN : MODE_AA_ODD; src = S->buf[0]; }
+    else { mode = aa_mode(S); src = S->buf[0]; }
     LBM_TRY(sim_launch(S, mode, true, src, src, S->steps_done, nullptr, p, of, orho, ou, st));
     if (partials) k_reduce_partials<<<1, 256, 0, st>>>(p, S->part_blocks, S->mon);
     LBM_CUDA(cudaGetLastError());
@@ -980,8 +1002,9 @@ lbm_status sim_create(const lbm_geometry* const* g, const lbm_sim_params* p, siz
     // node ids start at kLatticeSlack and the arrays end kLatticeSlack ids
     // after the last node: the paired kernel reads up to three ids beyond a
     // chunk's window for node slots it discards
-    int64_t node_off = kLatticeSlack, out_off = 0, nch = 0, nch2 = 0, nmask = 0;
-    std::vector<int64_t> lat_off(1, node_off), chunk_off(1, 0), chunk2_off(1, 0), mask_off(1, 0);
+    int64_t node_off = kLatticeSlack, out_off = 0, nch = 0, nch2[3] = {0, 0, 0}, nmask = 0;
+    std::vector<int64_t> lat_off(1, node_off), chunk_off(1, 0), mask_off(1, 0);
+    std::vector<int64_t> chunk2_off[3] = {{0}, {0}, {0}};
     S->inst_off.push_back(0);
     for (size_t i = 0; i < n; ++i) {
         builds.emplace_back(new InstBuild());
@@ -991,24 +1014,26 @@ lbm_status sim_create(const lbm_geometry* const* g, const lbm_sim_params* p, siz
         node_off += B.N;
         out_off += B.NF;
         nch += B.nchunks;
-        nch2 += B.nchunks2;
+        for (int k = 0; k < 3; ++k) nch2[k] += B.nchunks2[k];
         nmask += B.nmask;
         zall.insert(zall.end(), B.zslots.begin(), B.zslots.end());
         S->inst_off.push_back(out_off);
         lat_off.push_back(node_off);
         chunk_off.push_back(nch);
-        chunk2_off.push_back(nch2);
+        for (int k = 0; k < 3; ++k) chunk2_off[k].push_back(nch2[k]);
         mask_off.push_back(nmask);
     }
     S->N = node_off + kLatticeSlack;
     S->NF = out_off;
     S->nchunks = nch;
-    S->nchunks2 = nch2;
+    for (int k = 0; k < 3; ++k) S->nchunks2s[k] = nch2[k];
     S->nmask = nmask;
     S->nz = (int64_t)zall.size();
     // concatenate per-instance arrays
     LBM_CUDA(cudaMalloc(&S->chunks, sizeof(Chunk) * std::max<int64_t>(nch, 1)));
-    if (S->store != ST_F64) LBM_CUDA(cudaMalloc(&S->chunks2, sizeof(Chunk) * std::max<int64_t>(nch2, 1)));
+    if (S->store != ST_F64)
+        for (int k = 0; k < 3; ++k)
+            LBM_CUDA(cudaMalloc(&S->chunks2s[k], sizeof(Chunk) * std::max<int64_t>(nch2[k], 1)));
     LBM_CUDA(cudaMalloc(&S->mmask, sizeof(uint32_t) * std::max<int64_t>(nmask, 1)));
     LBM_CUDA(cudaMalloc(&S->node_grid, sizeof(int64_t) * S->NF));
     LBM_CUDA(cudaMalloc(&S->out_pos, sizeof(int32_t) * S->N));
@@ -1017,9 +1042,10 @@ lbm_status sim_create(const lbm_geometry* const* g, const lbm_sim_params* p, siz
         const InstBuild& B = *builds[i];
         LBM_CUDA(cudaMemcpyAsync(S->chunks + chunk_off[i], B.chunks.p, sizeof(Chunk) * B.nchunks,
                                  cudaMemcpyDeviceToDevice, st));
-        if (S->store != ST_F64 && B.nchunks2)
-            LBM_CUDA(cudaMemcpyAsync(S->chunks2 + chunk2_off[i], B.chunks2.p, sizeof(Chunk) * B.nchunks2,
-                                     cudaMemcpyDeviceToDevice, st));
+        for (int k = 0; k < 3 && S->store != ST_F64; ++k)
+            if (B.nchunks2[k])
+                LBM_CUDA(cudaMemcpyAsync(S->chunks2s[k] + chunk2_off[k][i], B.chunks2[k].p,
+                                         sizeof(Chunk) * B.nchunks2[k], cudaMemcpyDeviceToDevice, st));
         if (B.nmask)
             LBM_CUDA(cudaMemcpyAsync(S->mmask + mask_off[i], B.mmask.p, sizeof(uint32_t) * B.nmask,
                                      cudaMemcpyDeviceToDevice, st));
@@ -1028,6 +1054,7 @@ lbm_status sim_create(const lbm_geometry* const* g, const lbm_sim_params* p, siz
         LBM_CUDA(cudaMemcpyAsync(S->out_pos + lat_off[i], B.out_pos.p, sizeof(int32_t) * B.N, cudaMemcpyDeviceToDevice,
                                  st));
     }
+    select_piece(S.get(), S->piece);       // after the piece tables exist
     LBM_CUDA(cudaMalloc(&S->zslots, sizeof(ZSlot) * std::max<size_t>(zall.size(), 1)));
     if (!zall.empty())
         LBM_CUDA(cudaMemcpyAsync(S->zslots, zall.data(), sizeof(ZSlot) * zall.size(), cudaMemcpyHostToDevice, st));
@@ -1230,7 +1257,7 @@ lbm_status lbm_sim_step(lbm_sim* S, int64_t nsteps, uint32_t flags, void* stream
     if ((flags & LBM_STEP_GRAPH) && nsteps >= 4) {
         // state parity must match the captured graph: pull buffer index and
         // AA step parity both return to their start after an even step count
-        if ((S->steps_done & 1) || (S->pattern == LBM_PULL && S->cur != 0)) {
+        if (S->pattern == LBM_PULL ? S->cur != 0 : aa_mode(S) != MODE_AA_EVEN) {
             LBM_TRY(sim_one_step(S, S->steps_done, nullptr, st, true));
             --left;
         }
@@ -1279,32 +1306,106 @@ lbm_status lbm_sim_step(lbm_sim* S, int64_t nsteps, uint32_t flags, void* stream
     return LBM_OK;
 }
 
+// Pattern conversion.  After an AA even launch slot opp(q) of node x holds
+// f*_q(x), the post-collision population the pull pattern keeps in slot q of
+// its source lattice (and the bounced values of boundary nodes sit where each
+// pattern's next launch reads them); so the two states differ by a
+// permutation of the population planes.  AA -> pull needs that state (the
+// next AA launch odd); pull -> AA always works and sets aa_phase so that the
+// next AA launch is the odd one.
+static lbm_status convert_pattern(lbm_sim* S, int pattern, cudaStream_t st) {
+    if (pattern == S->pattern) return LBM_OK;
+    const size_t es = store_bytes(S->store), plane = (size_t)S->stride * es;
+    const size_t bytes = plane * S->Q;
+    auto swap_planes = [&](void* dst, const void* src) -> lbm_status {
+        for (int q = 0; q < S->Q; ++q) {
+            const int o = S->Q == 19 ? Lat<19>::opp(q) : Lat<27>::opp(q);
+            LBM_CUDA(cudaMemcpyAsync((char*)dst + (size_t)q * plane, (const char*)src + (size_t)o * plane, plane,
+                                     cudaMemcpyDeviceToDevice, st));
+        }
+        return LBM_OK;
+    };
+    if (pattern == LBM_PULL) {
+        if (S->npl == 4) return fail(LBM_ERR_ARG, "the four-level kernel runs the AA pattern only");
+        if (aa_mode(S) != MODE_AA_ODD)
+            return fail(LBM_ERR_STATE, "AA -> pull needs the state after an even (node-local) launch; step once more");
+        if (!S->buf[1] && cudaMalloc(&S->buf[1], bytes) != cudaSuccess) {
+            cudaGetLastError();
+            S->buf[1] = nullptr;
+            return fail(LBM_ERR_NOMEM, "no room for the pull pattern's second lattice (%zu bytes)", bytes);
+        }
+        LBM_TRY(swap_planes(S->buf[1], S->buf[0]));
+        S->cur = 1;
+    } else {
+        void* src = S->buf[S->cur];
+        void* dst = S->buf[1 - S->cur];
+        LBM_TRY(swap_planes(dst, src));
+        LBM_CUDA(cudaStreamSynchronize(st));
+        cudaFree(src);                     // the AA pattern keeps one lattice
+        S->buf[0] = dst;
+        S->buf[1] = nullptr;
+        S->cur = 0;
+        S->aa_phase = (int)((S->steps_done + 1) & 1);     // the next launch is an odd one
+    }
+    LBM_CUDA(cudaStreamSynchronize(st));
+    S->pattern = pattern;
+    free_graph(S);
+    return LBM_OK;
+}
+
+lbm_status lbm_sim_set_pattern(lbm_sim* S, int32_t pattern, void* stream) {
+    if (!S || (pattern != LBM_PULL && pattern != LBM_AA)) return fail(LBM_ERR_ARG, "lbm_sim_set_pattern: bad argument");
+    clear_error();
+    LBM_TRY(check_timeout(S, (cudaStream_t)stream));
+    return convert_pattern(S, pattern, (cudaStream_t)stream);
+}
+
 lbm_status lbm_sim_autotune(lbm_sim* S, int32_t launches, void* stream, lbm_tune_entry* entries, size_t cap,
                             size_t* n) {
     if (!S || launches < 2) return fail(LBM_ERR_ARG, "lbm_sim_autotune: null handle or fewer than 2 launches");
     clear_error();
     cudaStream_t st = (cudaStream_t)stream;
-    // scratch copy of the state: the candidates run on it, the simulation is untouched
+    LBM_TRY(check_timeout(S, st));
+    // scratch copies of the state: the candidates run on them, the simulation is untouched
     const size_t bytes = (size_t)S->stride * S->Q * store_bytes(S->store);
-    const int nb = S->pattern == LBM_PULL ? 2 : 1;
+    // patterns: the current one; the other one where the state converts now
+    // (AA -> pull after an even launch; pull -> AA always) and its memory fits
+    std::vector<int> patterns = {S->pattern};
+    if (S->npl != 4 && (S->pattern == LBM_PULL || aa_mode(S) == MODE_AA_ODD))
+        patterns.push_back(S->pattern == LBM_PULL ? LBM_AA : LBM_PULL);
     void* scratch[2] = {nullptr, nullptr};
-    for (int b = 0; b < nb; ++b)
+    const bool need2 = std::find(patterns.begin(), patterns.end(), (int)LBM_PULL) != patterns.end();
+    for (int b = 0; b < (need2 ? 2 : 1); ++b)
         if (cudaMalloc(&scratch[b], bytes) != cudaSuccess) {
-            if (scratch[0]) cudaFree(scratch[0]);
             cudaGetLastError();
-            return fail(LBM_ERR_NOMEM, "lbm_sim_autotune: no room for a scratch copy of the state (%zu bytes)", bytes);
+            scratch[b] = nullptr;
+            if (b == 0) return fail(LBM_ERR_NOMEM, "lbm_sim_autotune: no room for a scratch copy of the state (%zu bytes)", bytes);
+            patterns = {S->pattern};        // no room for pull's second lattice: keep the pattern
+            if (S->pattern == LBM_PULL) {
+                cudaFree(scratch[0]);
+                return fail(LBM_ERR_NOMEM, "lbm_sim_autotune: no room for two scratch lattices (%zu bytes)", bytes);
+            }
         }
-    struct Cand { int npl, staging, wpb; float ms; };
+    struct Cand { int pattern, npl, staging, wpb, piece; float ms; };
     std::vector<Cand> cands;
     const int wpbs[4] = {1, 2, 4, 8};
-    for (int w : wpbs) cands.push_back({1, 1, w, 0.f});
-    for (int w : wpbs) cands.push_back({1, 0, w, 0.f});
-    if (S->store != ST_F64)
-        for (int w : wpbs) cands.push_back({2, 1, w, 0.f});
-    const int save_npl = S->npl, save_staging = S->staging, save_wpb = S->wpb;
+    for (int pat : patterns) {
+        if (S->npl == 4) {
+            // the four-level lattice and its state layout serve the four-level kernel only
+            for (int w : wpbs) cands.push_back({pat, 4, 1, w, S->piece, 0.f});
+            continue;
+        }
+        for (int w : wpbs) cands.push_back({pat, 1, 1, w, S->piece, 0.f});
+        for (int w : wpbs) cands.push_back({pat, 1, 0, w, S->piece, 0.f});
+        if (S->store != ST_F64)
+            for (int pc : {8, 16, 32})
+                for (int w : wpbs) cands.push_back({pat, 2, 1, w, pc, 0.f});
+    }
+    const int save_pattern = S->pattern, save_npl = S->npl, save_staging = S->staging, save_wpb = S->wpb,
+              save_piece = S->piece;
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     lbm_status res = LBM_OK;
-    auto run = [&](int count, int parity0) -> lbm_status {
+    auto run = [&](int count) -> lbm_status {
         for (int i = 0; i < count; ++i) {
             Partials np = {nullptr, nullptr, nullptr, nullptr, nullptr};
             lbm_status s;
@@ -1312,8 +1413,8 @@ lbm_status lbm_sim_autotune(lbm_sim* S, int32_t launches, void* stream, lbm_tune
                 s = sim_launch(S, MODE_PULL, false, scratch[i & 1], scratch[1 - (i & 1)], S->steps_done + i, nullptr,
                                np, nullptr, nullptr, nullptr, st);
             else
-                s = sim_launch(S, ((parity0 + i) & 1) ? MODE_AA_ODD : MODE_AA_EVEN, false, scratch[0], scratch[0],
-                               S->steps_done + i, nullptr, np, nullptr, nullptr, nullptr, st);
+                s = sim_launch(S, ((S->steps_done + S->aa_phase + i) & 1) ? MODE_AA_ODD : MODE_AA_EVEN, false,
+                               scratch[0], scratch[0], S->steps_done + i, nullptr, np, nullptr, nullptr, nullptr, st);
             if (s != LBM_OK) return s;
         }
         return LBM_OK;
@@ -1325,12 +1426,12 @@ lbm_status lbm_sim_autotune(lbm_sim* S, int32_t launches, void* stream, lbm_tune
             res = fail(LBM_ERR_CUDA, "lbm_sim_autotune: set-up failed");
             break;
         }
-        const int parity0 = (int)(S->steps_done & 1);
         for (Cand& c : cands) {
-            S->npl = c.npl; S->staging = c.staging; S->wpb = c.wpb;
-            if ((res = run(2, parity0)) != LBM_OK) break;      // warm-up (even count keeps the AA parity)
+            S->pattern = c.pattern; S->npl = c.npl; S->staging = c.staging; S->wpb = c.wpb;
+            if (c.npl == 2) select_piece(S, c.piece);
+            if ((res = run(2)) != LBM_OK) break;      // warm-up (even count keeps the AA parity)
             cudaEventRecord(e0, st);
-            if ((res = run(launches & ~1, parity0)) != LBM_OK) break;
+            if ((res = run(launches & ~1)) != LBM_OK) break;
             cudaEventRecord(e1, st);
             if (cudaEventSynchronize(e1) != cudaSuccess) { res = fail(LBM_ERR_CUDA, "lbm_sim_autotune: timing"); break; }
             cudaEventElapsedTime(&c.ms, e0, e1);
@@ -1339,13 +1440,16 @@ lbm_status lbm_sim_autotune(lbm_sim* S, int32_t launches, void* stream, lbm_tune
     } while (false);
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
-    for (int b = 0; b < nb; ++b) cudaFree(scratch[b]);
-    S->npl = save_npl; S->staging = save_staging; S->wpb = save_wpb;
+    for (void* b : scratch) if (b) cudaFree(b);
+    S->pattern = save_pattern; S->npl = save_npl; S->staging = save_staging; S->wpb = save_wpb;
+    if (S->npl != 4) select_piece(S, save_piece);
     if (res != LBM_OK) return res;
     LBM_TRY(check_timeout(S, st));
     const Cand* best = &cands[0];
     for (const Cand& c : cands) if (c.ms < best->ms) best = &c;
+    if (best->pattern != S->pattern) LBM_TRY(convert_pattern(S, best->pattern, st));
     S->npl = best->npl; S->staging = best->staging; S->wpb = best->wpb;
+    if (S->npl == 2) select_piece(S, best->piece);
     free_graph(S);                         // the captured launches used the old shape
     if (n) *n = cands.size();
     if (entries)
@@ -1354,6 +1458,8 @@ lbm_status lbm_sim_autotune(lbm_sim* S, int32_t launches, void* stream, lbm_tune
             entries[i].staging = cands[i].staging;
             entries[i].warps_per_block = cands[i].wpb;
             entries[i].chosen = &cands[i] == best ? 1 : 0;
+            entries[i].pattern = cands[i].pattern;
+            entries[i].piece_slots = cands[i].npl == 2 ? cands[i].piece : 0;
             entries[i].ms_per_launch = cands[i].ms;
         }
     return LBM_OK;
@@ -1491,6 +1597,13 @@ lbm_status lbm_sim_set_wait_limit(lbm_sim* S, uint32_t polls) {
     if (!S) return fail(LBM_ERR_ARG, "lbm_sim_set_wait_limit: null handle");
     S->spin_limit = polls;
     free_graph(S);                         // captured launches carry the old limit
+    return LBM_OK;
+}
+
+lbm_status lbm_sim_test_stall(lbm_sim* S, int32_t enable) {
+    if (!S) return fail(LBM_ERR_ARG, "lbm_sim_test_stall: null handle");
+    S->stall_first = enable ? 1 : 0;
+    free_graph(S);
     return LBM_OK;
 }
 
@@ -1685,8 +1798,9 @@ void lbm_snapshot_destroy(lbm_snapshot* P) {
 // (the plane-major device array, stride * Q values of the storage type).
 namespace {
 struct CkptHeader {
-    char magic[8];            // "LBMCKPT1"
+    char magic[8];            // "LBMCKPT2"
     int32_t Q, store, pattern, n_inst;
+    int32_t aa_phase, pad;
     int64_t N, NF, stride, nchunks, steps_done;
     uint64_t grid_hash;       // FNV-1a of the output nodes' grid indices
     uint64_t bytes;
@@ -1698,8 +1812,9 @@ uint64_t fnv1a(const void* p, size_t n, uint64_t h = 1469598103934665603ull) {
 }
 lbm_status ckpt_header(lbm_sim* S, CkptHeader& h) {
     std::memset(&h, 0, sizeof h);
-    std::memcpy(h.magic, "LBMCKPT1", 8);
+    std::memcpy(h.magic, "LBMCKPT2", 8);
     h.Q = S->Q; h.store = S->store; h.pattern = S->pattern; h.n_inst = (int32_t)S->n_inst;
+    h.aa_phase = S->aa_phase;
     h.N = S->N; h.NF = S->NF; h.stride = S->stride; h.nchunks = S->nchunks; h.steps_done = S->steps_done;
     std::vector<int64_t> g((size_t)S->NF);
     LBM_CUDA(cudaMemcpy(g.data(), S->node_grid, sizeof(int64_t) * S->NF, cudaMemcpyDeviceToHost));
@@ -1745,7 +1860,7 @@ lbm_status lbm_sim_restart(lbm_sim* S, const char* path, void* stream) {
     const bool got = std::fread(&h, sizeof h, 1, f) == 1;
     lbm_status hs = ckpt_header(S, mine);
     if (hs != LBM_OK) { std::fclose(f); return hs; }
-    if (!got || std::memcmp(h.magic, "LBMCKPT1", 8) != 0) {
+    if (!got || std::memcmp(h.magic, "LBMCKPT2", 8) != 0) {
         std::fclose(f);
         return fail(LBM_ERR_PARSE, "%s is not a checkpoint of this engine", path);
     }
@@ -1774,6 +1889,8 @@ lbm_status lbm_sim_restart(lbm_sim* S, const char* path, void* stream) {
     std::fclose(f);
     S->cur = 0;
     S->steps_done = h.steps_done;
+    S->aa_phase = h.aa_phase;
+    free_graph(S);
     return LBM_OK;
 }
 
@@ -1782,7 +1899,7 @@ void lbm_sim_destroy(lbm_sim* S) {
     free_graph(S);
     for (void* b : S->buf) if (b) cudaFree(b);
     if (S->chunks) cudaFree(S->chunks);
-    if (S->chunks2) cudaFree(S->chunks2);
+    for (Chunk* c : S->chunks2s) if (c) cudaFree(c);
     if (S->wall_pos) cudaFree(S->wall_pos);
     if (S->zslots) cudaFree(S->zslots);
     if (S->lists) cudaFree(S->lists);

@@ -21,7 +21,10 @@
 // the host as LBM_ERR_TIMEOUT), drains the stages still in flight with waits
 // bounded by kSpinLimit each, and stops.  A drain that gives up too sets bit 1:
 // that only follows a stall of the copy hardware itself, and the warp may then
-// exit with bulk copies still writing into its shared memory.
+// exit with bulk copies still writing into its shared memory.  For failure
+// tests (a.stall_first) each warp leaves its first stage unissued -- no copy,
+// no arrival -- so that stage's wait cannot complete: the warp gives up, and
+// its drain skips that stage (nothing is in flight there).
 #pragma once
 #include "step_kernel.cuh"
 
@@ -158,7 +161,7 @@ __global__ void __launch_bounds__(256) k_step_tma(StepArgs a, int32_t* err) {
 
     uint32_t dw = load_desc(0);
     for (int k = 0; k < kStages - 1; ++k) {
-        if (chunk_of(k) < a.nchunks) issue(k, dw);
+        if (chunk_of(k) < a.nchunks && !(k == 0 && a.stall_first)) issue(k, dw);
         dw = load_desc(k + 1);
     }
     uint32_t parity = 0;   // bit s: phase parity of stage s
@@ -184,6 +187,7 @@ __global__ void __launch_bounds__(256) k_step_tma(StepArgs a, int32_t* err) {
                 // record the failure, then drain (bounded) every stage still in flight
                 bool drained = true;
                 for (int64_t j = k; j < k + kStages && chunk_of(j) < a.nchunks; ++j) {
+                    if (j == 0 && a.stall_first) continue;      // never issued
                     const int sj = (int)(j % kStages);
                     const uint32_t bj = smem_addr(ring + sj * LY::BYTES + LY::BAR);
                     uint32_t t = 0;

@@ -389,14 +389,19 @@ class Simulation:
                 "max_speed": m.max_speed, "nonfinite": bool(m.nonfinite)}
 
     def autotune(self, launches=20):
-        """Times the step-kernel variants on a scratch copy of the state and
-        keeps the fastest; returns [(nodes_per_lane, staging, warps_per_block,
-        ms_per_launch, chosen)]."""
-        ents = (_capi.TuneEntry * 16)()
+        """Times the step-kernel variants (kernel, staging, block size, piece
+        size, streaming pattern) on scratch copies of the state and keeps the
+        fastest; returns [(nodes_per_lane, staging, warps_per_block,
+        ms_per_launch, chosen, pattern, piece_slots)]."""
+        ents = (_capi.TuneEntry * 64)()
         n = C.c_size_t()
-        check(load().lbm_sim_autotune(self._h, int(launches), self._stream, ents, 16, C.byref(n)))
-        return [(e.nodes_per_lane, e.staging, e.warps_per_block, e.ms_per_launch, bool(e.chosen))
-                for e in ents[:n.value]]
+        check(load().lbm_sim_autotune(self._h, int(launches), self._stream, ents, 64, C.byref(n)))
+        return [(e.nodes_per_lane, e.staging, e.warps_per_block, e.ms_per_launch, bool(e.chosen),
+                 {_capi.PULL: "pull", _capi.AA: "aa"}[e.pattern], e.piece_slots) for e in ents[:min(n.value, 64)]]
+
+    def set_pattern(self, pattern):
+        """Converts the state to another streaming pattern ("pull" or "aa")."""
+        check(load().lbm_sim_set_pattern(self._h, {"pull": _capi.PULL, "aa": _capi.AA}[pattern], self._stream))
 
     def set_divergence_tolerance(self, tol):
         check(load().lbm_sim_set_divergence_tolerance(self._h, float(tol)))
@@ -404,6 +409,10 @@ class Simulation:
     def set_wait_limit(self, polls):
         """Poll limit of the TMA-staged kernel's bounded waits (0 = default)."""
         check(load().lbm_sim_set_wait_limit(self._h, int(polls)))
+
+    def test_stall(self, enable):
+        """Failure-test hook: the TMA-staged kernel's waits on each warp's first stage run out."""
+        check(load().lbm_sim_test_stall(self._h, 1 if enable else 0))
 
     def wall_shear_stress(self):
         """Wall shear stress at every wall node, wall-list order (ComputeWallShearStress)."""

@@ -142,13 +142,20 @@ def test_autotune_keeps_state_and_results(pattern):
     b.step(5)
     f_before = b.fields()[0]
     res = b.autotune(launches=6)
-    assert len(res) == 12 and sum(r[4] for r in res) == 1
+    # both patterns (an AA state after an even launch converts), one node per
+    # lane direct / TMA-staged and two nodes per lane with 8-, 16-, 32-slot
+    # pieces, 1-8 warps per block
+    assert len(res) == 40 and sum(r[4] for r in res) == 1
+    assert {r[5] for r in res} == {"aa", "pull"} and {r[6] for r in res if r[0] == 2} == {8, 16, 32}
     assert all(r[3] > 0 for r in res)
     assert b.info().steps_done == 5
     assert np.array_equal(b.fields()[0], f_before)
     chosen = [r for r in res if r[4]][0]
     info = b.info()
     assert (info.nodes_per_lane, info.warps_per_block) == (chosen[0], chosen[2])
+    assert info.pattern == {"pull": _capi.PULL, "aa": _capi.AA}[chosen[5]]
+    if chosen[0] == 2:
+        assert info.piece_slots == chosen[6]
     a.step(40, graph=True)
     b.step(40, graph=True)
     assert rel_l2(b.fields()[0], a.fields()[0]) < 1e-6
@@ -210,3 +217,32 @@ def test_automatic_run_axis_has_fewer_chunks(make):
     auto = Simulation(geom, c.tau, specs, precision="f16s", pattern="aa").info()
     assert auto.n_chunks == min(n.values())
     assert n[auto.run_axis] == auto.n_chunks
+
+
+@pytest.mark.parametrize("precision", ["f16s", "f32", "f64"])
+def test_pattern_conversion_keeps_results(precision):
+    """lbm_sim_set_pattern: an AA state after an even launch is the pull
+    state with its planes permuted, so a run that switches AA -> pull (after
+    an odd number of steps) or pull -> AA (any time) continues with the same
+    bits as a run that never switched."""
+    c = cases.vessel(4002)
+    geom = c.geometry()
+    specs = c.boundary_specs(geom)
+    npl = 1 if precision == "f64" else 2
+    mk = lambda pat: Simulation(geom, c.tau, specs, precision=precision, pattern=pat, nodes_per_lane=npl, staging=1)
+    ref = mk("aa")
+    ref.step(48, graph=True)
+    a = mk("aa")
+    a.step(7)
+    a.set_pattern("pull")
+    assert a.info().pattern == _capi.PULL
+    a.step(22, graph=True)
+    a.set_pattern("aa")              # pull -> AA with the step count odd
+    assert a.info().pattern == _capi.AA
+    a.step(19, graph=True)
+    assert np.array_equal(a.fields()[0], ref.fields()[0])
+    b = mk("aa")
+    b.step(6)
+    with pytest.raises(_capi.LbmError) as e:
+        b.set_pattern("pull")        # after an odd launch: not a pull state
+    assert e.value.status == _capi.ERR_STATE

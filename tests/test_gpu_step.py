@@ -221,11 +221,12 @@ def test_corrections_act_on_boundary_nodes_first():
 
 
 def test_bounded_wait_runs_out_and_the_handle_recovers(tmp_path):
-    """The TMA-staged kernel's mbarrier waits are bounded: with a limit of one
-    non-blocking test the staged copies cannot have arrived, the warps record
-    the give-up and drain their copies, the next monitor call reports
-    LBM_ERR_TIMEOUT once; with the default limit restored and the state
-    restored from a checkpoint the run continues bit for bit."""
+    """The TMA-staged kernel's mbarrier waits are bounded.  With the
+    failure-test hook each warp's first stage is never issued (no copy, no
+    arrival): its wait, limited to 1000 non-blocking tests, runs out; the warp
+    records it, drains its other stages and stops; the next monitor call
+    reports LBM_ERR_TIMEOUT, once.  With the hook off, the default limit and
+    the state restored from a checkpoint, the run continues bit for bit."""
     c = cases.pipe()
     geom = c.geometry()
     specs = c.boundary_specs(geom)
@@ -235,12 +236,14 @@ def test_bounded_wait_runs_out_and_the_handle_recovers(tmp_path):
     sim.step(4)
     path = str(tmp_path / "w.ckpt")
     sim.checkpoint(path)
-    sim.set_wait_limit(1)
+    sim.set_wait_limit(1000)
+    sim.test_stall(True)
     sim.step(2)
     with pytest.raises(_capi.LbmError) as e:
         sim.monitors()
     assert e.value.status == _capi.ERR_TIMEOUT
     sim.monitors()          # reported once: this call succeeds
+    sim.test_stall(False)
     sim.set_wait_limit(0)
     sim.restart(path)
     sim.step(6)
