@@ -358,9 +358,15 @@ def gpu_arm(args, rank, world):
     # --- batched: the 64-vessel ensemble in one launch per step --------------
     batched = None
     if not args.no_batch:
+        # the 64 vessels are independent: under torchrun each rank advances its
+        # share of them (balanced by fluid nodes, no exchange between ranks)
+        from pv2013_gb300.shard import shard
         ens = cases.ensemble(64)
-        egeo = [c.geometry() for c in ens]
-        enf = sum(g.info.n_fluid for g in egeo)
+        egeo_all = [c.geometry() for c in ens]
+        mine = shard([g.info.n_fluid for g in egeo_all], rank, world)
+        ens = [ens[i] for i in mine]
+        egeo = [egeo_all[i] for i in mine]
+        enf = sum(g.info.n_fluid for g in egeo_all)      # all ranks' nodes
         esim = Simulation(egeo, [c.tau for c in ens], [c.boundary_specs(g) for c, g in zip(ens, egeo)],
                           precision="f16s", pattern=args.pattern, piece_slots=args.piece_slots)
         esim.step(1)                         # after an even launch both patterns are candidates
@@ -369,13 +375,14 @@ def gpu_arm(args, rank, world):
         einfo = esim.info()
         batched = {"workload": "ensemble of 64 tortuous vessels (seeds 4000-4063), per-instance tau, inlet amplitude "
                                "and period, FP16-shifted AA, one launch per step",
-                   "fluid_nodes": enf, "steps": args.batch_steps, "mlups": enf * args.batch_steps / esec / 1e6 * world,
+                   "fluid_nodes": enf, "steps": args.batch_steps, "mlups": enf * args.batch_steps / esec / 1e6,
+                   "sharding": f"{len(mine)} of 64 vessels on this rank, {world} rank(s), no exchange",
                    "ms_per_step": esec / args.batch_steps * 1e3,
                    "kernel": {"nodes_per_lane": einfo.nodes_per_lane, "piece_slots": einfo.piece_slots,
                               "warps_per_block": einfo.warps_per_block,
                               "pattern": {0: "pull", 1: "aa"}[einfo.pattern],
                               "candidates": len(tuned)}}
-        del esim, egeo
+        del esim, egeo, egeo_all
 
     # --- roofline of the step kernel ------------------------------------------
     launch_s = sec16 / args.steps
