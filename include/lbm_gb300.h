@@ -319,9 +319,10 @@ lbm_status lbm_sim_fields(lbm_sim* s, double* rho, double* u, double* f, size_t 
  * own (at most 524288 nodes; larger lattices: LBM_ERR_ARG) and copies them to
  * the caller's buffers, with no cudaMalloc or cudaFree.  The array is shared
  * by every call and keeps the last call's values, so calls whose GPU work
- * overlaps race.  The first call on a device sets the array up (make it
- * before any stream capture); the handle's device must be current.
- * No counterpart in the reference. */
+ * overlaps race.  The handle's device must be current.  The call
+ * synchronises `stream` before it returns, so it cannot be used inside a
+ * stream capture; the first call on a device may load the library's device
+ * module.  No counterpart in the reference. */
 lbm_status lbm_sim_fields_noalloc(lbm_sim* s, double* rho, double* u, size_t n_nodes, void* stream);
 /* Node positions: x-major grid index of every node (per instance, concatenated). */
 lbm_status lbm_sim_nodes(const lbm_sim* s, int64_t* grid_index, size_t cap);

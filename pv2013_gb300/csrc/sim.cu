@@ -1521,29 +1521,21 @@ lbm_status lbm_sim_fields(lbm_sim* S, double* rho, double* u, double* f, size_t 
 // call wrote: calls whose GPU work overlaps (other threads, other streams)
 // race on it.  Each call writes every value it copies out (one rho and one u
 // per fluid node), so nothing has to be cleared between calls.
-// The first call on a device looks up the array's device address with that
-// device current (cudaGetSymbolAddress, which may load the module); make that
-// first call before any stream capture.
+// Each call looks up the array's device address with the handle's device
+// current (cudaGetSymbolAddress: a table lookup once the module is loaded; the
+// first call on a device may load it).  The address is not cached, so a call
+// after a device reset or a new primary context uses the module's new address.
 static constexpr int64_t kStaticFieldNodes = int64_t(1) << 19;
 static __device__ __align__(256) double g_field_scratch[4 * kStaticFieldNodes];
 
 namespace {
-constexpr int kMaxFieldDevices = 64;
-std::mutex g_field_mu;
-double* g_field_ptr[kMaxFieldDevices] = {};
-
-// device address of g_field_scratch on device `dev` (current), looked up once
-lbm_status field_scratch(int dev, double** out) {
-    std::lock_guard<std::mutex> lock(g_field_mu);
-    if (dev < 0 || dev >= kMaxFieldDevices) return fail(LBM_ERR_ARG, "device %d out of range", dev);
-    if (!g_field_ptr[dev]) {
-        void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_field_scratch);
-        if (e != cudaSuccess || !p)
-            return fail(LBM_ERR_CUDA, "cudaGetSymbolAddress(field scratch): %s", cudaGetErrorString(e));
-        g_field_ptr[dev] = (double*)p;
-    }
-    *out = g_field_ptr[dev];
+// device address of g_field_scratch on the current device
+lbm_status field_scratch(double** out) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_field_scratch);
+    if (e != cudaSuccess || !p)
+        return fail(LBM_ERR_CUDA, "cudaGetSymbolAddress(field scratch): %s", cudaGetErrorString(e));
+    *out = (double*)p;
     return LBM_OK;
 }
 }  // namespace
@@ -1561,7 +1553,7 @@ lbm_status lbm_sim_fields_noalloc(lbm_sim* S, double* rho, double* u, size_t n_n
     if (dev != S->dev)
         return fail(LBM_ERR_STATE, "lbm_sim_fields_noalloc: device %d is current, the handle lives on %d", dev, S->dev);
     double* scratch = nullptr;
-    LBM_TRY(field_scratch(dev, &scratch));
+    LBM_TRY(field_scratch(&scratch));
     cudaStream_t st = (cudaStream_t)stream;
     double* drho = scratch;
     double* du = scratch + kStaticFieldNodes;

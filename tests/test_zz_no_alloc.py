@@ -60,6 +60,28 @@ def test_noalloc_fields_equal_allocating_fields():
     _check_same(*_fields_pair(lib, sv))
 
 
+def test_noalloc_fields_leave_free_device_memory_unchanged():
+    """The promise itself: after a warm-up call, further calls change the
+    device's free memory by nothing (cudaMemGetInfo before and after)."""
+    import torch
+    lib = _capi.load()
+    c = cases.pipe()
+    geom = c.geometry()
+    sim = Simulation(geom, c.tau, c.boundary_specs(geom), precision="f32", pattern="aa")
+    sim.step(2)
+    n = sim.info().n_nodes
+    r, u = np.empty(n), np.empty((n, 3))
+    assert lib.lbm_sim_fields_noalloc(sim._h, _ptr(r), _ptr(u), n, None) == 0, _capi.last_error()
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for _ in range(5):
+        sim.step(1)
+        assert lib.lbm_sim_fields_noalloc(sim._h, _ptr(r), _ptr(u), n, None) == 0, _capi.last_error()
+        free1, _ = torch.cuda.mem_get_info()
+        assert free1 == free0
+    assert np.isfinite(r).all()
+
+
 def test_noalloc_fields_reject_oversized_lattice():
     lib = _capi.load()
     c = cases.pipe(radius=40.0, length=200.0, segments=96, ny=208, nxz=88)
