@@ -437,6 +437,44 @@ __global__ void k_col_fill2(FillArgs A) {
     }
 }
 
+// Paired pieces regrouped within windows of `win` consecutive pieces (at most
+// 1024; 16 warps' worth by default): interior pieces (every slot a fluid
+// node, no boundary node) first, then the others, each group in its original
+// order.  The paired kernel's boundary work (missing-population fix-ups,
+// per-half stores) is decided per warp, so warps made only of interior pieces
+// skip it; the window keeps a warp's pieces within a few KB of each other in
+// every plane.  Every piece carries its own ids and slots, so the order is free.
+constexpr int kGroupMax = 1024;
+constexpr int kGroupWarps = 16;         // window: this many warps' pieces (16 * 8 8-slot pieces <= kGroupMax)
+__device__ __forceinline__ bool interior_piece(const Chunk& c) {
+    const uint32_t len = c.len_inst & 63u;
+    const uint32_t full = len >= 32 ? 0xffffffffu : (1u << len) - 1u;
+    return c.bmask == 0u && c.zmask == 0u && c.vmask == full;
+}
+__global__ void __launch_bounds__(kGroupMax) k_group_pieces(const Chunk* __restrict__ in, Chunk* __restrict__ out,
+                                                            int64_t n, int win) {
+    __shared__ int cnt[kGroupMax / 32];
+    const int i = threadIdx.x;
+    for (int64_t w = blockIdx.x; w * win < n; w += gridDim.x) {
+        const int64_t j = w * win + i;
+        const bool have = i < win && j < n;
+        Chunk c;
+        bool inner = false;
+        if (have) { c = in[j]; inner = interior_piece(c); }
+        const uint32_t b = __ballot_sync(0xffffffffu, inner);
+        if ((i & 31) == 0) cnt[i >> 5] = __popc(b);
+        __syncthreads();
+        int ninner = 0, before = __popc(b & ((1u << (i & 31)) - 1u));
+        for (int k = 0; k < kGroupMax / 32; ++k) {
+            ninner += cnt[k];
+            if (k < (i >> 5)) before += cnt[k];
+        }
+        // the pieces of a window are items 0 .. m-1, so i items precede item i
+        if (have) out[w * win + (inner ? before : ninner + (i - before))] = c;
+        __syncthreads();
+    }
+}
+
 template <class T>
 __global__ void k_init_pop(T* __restrict__ a, int64_t stride, int Q, const double* __restrict__ val) {
     const int64_t n = stride * Q;
@@ -518,6 +556,8 @@ struct lbm_sim {
     Chunk* chunks2 = nullptr;      // paired chunk table in use (nodes_per_lane = 2): chunks2s[piece]
     int64_t nchunks2 = 0;
     Chunk* chunks2s[3] = {nullptr, nullptr, nullptr};   // paired tables of 8-, 16- and 32-slot pieces
+    Chunk* chunks2g = nullptr;     // the same pieces grouped (k_group_pieces): the AA odd launch's table
+    Chunk* chunks2gs[3] = {nullptr, nullptr, nullptr};
     int64_t nchunks2s[3] = {0, 0, 0};
     int aa_phase = 0;              // AA: launch n is an even (node-local) launch when n + aa_phase is even
     ZSlot* zslots = nullptr;
@@ -802,7 +842,7 @@ lbm_status sim_launch(lbm_sim* S, int mode, bool dry, void* src, void* dst, int6
     a.stall_first = S->stall_first;
     a.piece_lg = S->piece == 8 ? 2 : (S->piece == 16 ? 3 : 4);
     if (!dry && S->npl == 2) {
-        a.chunks = S->chunks2;
+        a.chunks = mode == MODE_AA_ODD ? S->chunks2g : S->chunks2;
         a.nchunks = S->nchunks2;
         switch (S->store) {
             case ST_F32: return launch_pair_f32(S->Q, mode, S->ra, a, S->wpb, st);
@@ -855,6 +895,7 @@ void select_piece(lbm_sim* S, int piece) {
     const int k = piece == 8 ? 0 : (piece == 16 ? 1 : 2);
     S->piece = piece;
     S->chunks2 = S->chunks2s[k];
+    S->chunks2g = S->chunks2gs[k];
     S->nchunks2 = S->nchunks2s[k];
 }
 
@@ -1053,6 +1094,18 @@ lbm_status sim_create(const lbm_geometry* const* g, const lbm_sim_params* p, siz
                                  cudaMemcpyDeviceToDevice, st));
         LBM_CUDA(cudaMemcpyAsync(S->out_pos + lat_off[i], B.out_pos.p, sizeof(int32_t) * B.N, cudaMemcpyDeviceToDevice,
                                  st));
+    }
+    // the AA odd launch's tables: interior pieces ahead of boundary pieces
+    // within windows of kGroupWarps warps (the node-local launches keep the
+    // memory order, which measured faster for them)
+    for (int k = 0; k < 3 && S->store != ST_F64; ++k) {
+        LBM_CUDA(cudaMalloc(&S->chunks2gs[k], sizeof(Chunk) * std::max<int64_t>(nch2[k], 1)));
+        if (nch2[k] == 0) continue;
+        const int win = kGroupWarps * (8 >> k);   // 8, 4, 2 pieces per warp for 8-, 16-, 32-slot pieces
+        const int64_t nwin = (nch2[k] + win - 1) / win;
+        k_group_pieces<<<(unsigned)std::min<int64_t>(nwin, 152 * 8), kGroupMax, 0, st>>>(S->chunks2s[k],
+                                                                                          S->chunks2gs[k], nch2[k], win);
+        LBM_CUDA(cudaGetLastError());
     }
     select_piece(S.get(), S->piece);       // after the piece tables exist
     LBM_CUDA(cudaMalloc(&S->zslots, sizeof(ZSlot) * std::max<size_t>(zall.size(), 1)));
@@ -1892,6 +1945,7 @@ void lbm_sim_destroy(lbm_sim* S) {
     for (void* b : S->buf) if (b) cudaFree(b);
     if (S->chunks) cudaFree(S->chunks);
     for (Chunk* c : S->chunks2s) if (c) cudaFree(c);
+    for (Chunk* c : S->chunks2gs) if (c) cudaFree(c);
     if (S->wall_pos) cudaFree(S->wall_pos);
     if (S->zslots) cudaFree(S->zslots);
     if (S->lists) cudaFree(S->lists);

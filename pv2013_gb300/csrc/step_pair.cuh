@@ -18,7 +18,11 @@
 //     bounced or initial values in the node's own slots (step_kernel.cuh).
 //     The AA odd launch's bounce-back source is the node's own word: boundary
 //     lanes copy their own words into shared memory (cp.async) while the
-//     gathers are in flight, so the fix-up waits on no further load.
+//     gathers are in flight, so the fix-up waits on no further load; the
+//     fix-up widens each population's two node flags to half-word masks
+//     with one byte permute.  The AA odd launch runs on a piece table in
+//     which interior pieces come first within every 16-warp window
+//     (k_group_pieces, sim.cu), so most warps take no boundary branch.
 // Chunk pieces start at even levels and hold up to 8, 16 or 32 node slots
 // (lbm_sim_params.piece_slots: shorter pieces leave fewer idle lanes where a
 // run ends, for 64 descriptor bytes per piece); a slot at either end may be a
@@ -201,6 +205,15 @@ __device__ __forceinline__ void zou_he_half(const StepArgs& a, int slot, typenam
 }
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// 0x0000ffff where bit 15 of f is set, | 0xffff0000 where bit 31 is set:
+// prmt with the sign-replicate selector bit (bytes 0-1 from the sign of byte
+// 1, bytes 2-3 from the sign of byte 3)
+__device__ __forceinline__ uint32_t half_masks(uint32_t f) {
+    uint32_t r;
+    asm("prmt.b32 %0, %1, 0, 0xBB99;" : "=r"(r) : "r"(f));
+    return r;
+}
 
 // identity the compiler cannot see through: the relaxation unpacks the words
 // again instead of keeping the first unpacked values alive
@@ -394,6 +407,8 @@ __global__ void __launch_bounds__(256) __maxnreg__((PairMaxReg<Q, S, MODE>::valu
     // the odd pattern's column bases go through shared memory (lane 0 of
     // each chunk wrote them): fewer registers held across the collision
     if constexpr (MODE == MODE_AA_ODD) __syncwarp();
+    // populations missing at some node of the warp (warp-uniform)
+    const uint32_t umiss = MODE == MODE_AA_ODD ? __reduce_or_sync(0xffffffffu, m_lo | m_hi) : 0u;
     // AA odd: missing populations (boundary nodes) take the bounced value from
     // the node's own word or the initial value (bounce_back_pop); only the
     // populations missing somewhere in the warp are visited (a per-lane loop
@@ -405,7 +420,6 @@ __global__ void __launch_bounds__(256) __maxnreg__((PairMaxReg<Q, S, MODE>::valu
             asm volatile("cp.async.wait_all;" ::: "memory");
             __syncwarp();
         }
-        const uint32_t umiss = __reduce_or_sync(0xffffffffu, m_lo | m_hi);
         if (umiss) {
             uint32_t wm = 0u;
             if (act) asm volatile("ld.global.nc.u32 %0, [%1];" : "=r"(wm) : "l"(&cw[0].z));   // wmask, read late
@@ -416,18 +430,36 @@ __global__ void __launch_bounds__(256) __maxnreg__((PairMaxReg<Q, S, MODE>::valu
             const bool fix_list = a.corr & LBM_FIX_LIST_NODES;
             const uint32_t b_lo = ((wm & 1u) || fix_list) ? (m_lo & keep) : 0u;
             const uint32_t b_hi = ((wm & 2u) || fix_list) ? (m_hi & keep) : 0u;
+            if constexpr (S == ST_F32) {
 #pragma unroll
-            for (int q = 0; q < Q; ++q) {
-                if (!((umiss >> q) & 1u)) continue;
-                const bool bl = (b_lo >> q) & 1u, bh = (b_hi >> q) & 1u;
-                const bool il = ((m_lo & ~b_lo) >> q) & 1u, ih = ((m_hi & ~b_hi) >> q) & 1u;
-                if (bl || bh) {
-                    const W own = buf[q * 32];
-                    if (bl) raw[q] = take_half<S>(raw[q], false, own);
-                    if (bh) raw[q] = take_half<S>(raw[q], true, own);
+                for (int q = 0; q < Q; ++q) {
+                    if (!((umiss >> q) & 1u)) continue;
+                    const bool bl = (b_lo >> q) & 1u, bh = (b_hi >> q) & 1u;
+                    const bool il = ((m_lo & ~b_lo) >> q) & 1u, ih = ((m_hi & ~b_hi) >> q) & 1u;
+                    if (bl || bh) {
+                        const W own = buf[q * 32];
+                        if (bl) raw[q] = take_half<S>(raw[q], false, own);
+                        if (bh) raw[q] = take_half<S>(raw[q], true, own);
+                    }
+                    if (il) raw[q] = init_half<S, Q>(raw[q], false, q);
+                    if (ih) raw[q] = init_half<S, Q>(raw[q], true, q);
                 }
-                if (il) raw[q] = init_half<S, Q>(raw[q], false, q);
-                if (ih) raw[q] = init_half<S, Q>(raw[q], true, q);
+            } else {
+                // 16-bit halves: the flags of population q for both nodes
+                // (lo node in bits 0-15, hi node in bits 16-31 of a flag word
+                // per 16 populations) shifted to bits 15 and 31, widened to
+                // half masks by a sign-replicating byte permute
+                const uint32_t i_lo = m_lo & ~b_lo, i_hi = m_hi & ~b_hi;
+                const uint32_t fb0 = (b_lo & 0xffffu) | (b_hi << 16), fb1 = (b_lo >> 16) | (b_hi & 0xffff0000u);
+                const uint32_t fi0 = (i_lo & 0xffffu) | (i_hi << 16), fi1 = (i_lo >> 16) | (i_hi & 0xffff0000u);
+#pragma unroll
+                for (int q = 0; q < Q; ++q) {
+                    if (!((umiss >> q) & 1u)) continue;
+                    const uint32_t mb = half_masks(q < 16 ? fb0 << (15 - q) : fb1 << (31 - q));
+                    const uint32_t mi = half_masks(q < 16 ? fi0 << (15 - q) : fi1 << (31 - q));
+                    // bounced halves from the node's own word; initial-value halves 0
+                    raw[q] = ((raw[q] & ~mb) | (buf[q * 32] & mb)) & ~mi;
+                }
             }
             __syncwarp();
         }
@@ -487,23 +519,32 @@ __global__ void __launch_bounds__(256) __maxnreg__((PairMaxReg<Q, S, MODE>::valu
         // ghost slots of the pair store nothing
         uint32_t vm, wm = 0u;
         asm volatile("ld.global.nc.u32 %0, [%1];" : "=r"(vm) : "l"(&cw[3].w));
-        if (__any_sync(__activemask(), (m_lo | m_hi) != 0u))
-            asm volatile("ld.global.nc.u32 %0, [%1];" : "=r"(wm) : "l"(&cw[0].z));   // wmask
+        if (umiss) asm volatile("ld.global.nc.u32 %0, [%1];" : "=r"(wm) : "l"(&cw[0].z));   // wmask
         vm = (vm >> (2 * t)) & 3u;
         wm = (wm >> (2 * t)) & 3u;
         const volatile int32_t* ks = ksm + pw * 8;
         // whole-word stores of the directions without a run-axis component
-        // only when no lane of the warp has a ghost slot or a bounce-back
-        // (a warp-uniform branch; per-lane it diverged, measured 1.5 % slower)
-        const bool wfast = __all_sync(__activemask(), vm == 3u && (m_lo | m_hi) == 0u);
+        // when every lane of the warp holds two fluid nodes (a warp-uniform
+        // branch; per lane it diverged, measured 1.5 % slower)
+        const bool wword = __all_sync(__activemask(), vm == 3u);
         collide2<Q, S>(raw, om, [&](int q, F2 v) {
             const int da = X::a(q), db = X::b(q), o = X::r(q);
             const uint32_t s = (uint32_t)((da == 0 && db == 0 ? n0 - 1 : ks[col8(da, db)]) + 1 + 2 * t);
-            const bool bl = (m_lo >> L::opp(q)) & 1u, bh = (m_hi >> L::opp(q)) & 1u;
-            const uint32_t pq = (uint32_t)q * st, po = (uint32_t)L::opp(q) * st;
-            if (o == 0 && wfast) {
-                stw<S>(D, (uint32_t)q * sw + (s >> 1), pack<S, Q>(v, q));
+            const uint32_t pq = (uint32_t)q * st;
+            if (umiss == 0u) {
+                // no node of the warp misses a population: every destination
+                // x + c_q exists (a warp-uniform test)
+                if (o == 0 && wword) {
+                    stw<S>(D, (uint32_t)q * sw + (s >> 1), pack<S, Q>(v, q));
+                } else {
+                    float l, h;
+                    f2split(v, l, h);
+                    if (vm & 1u) st_one<S, Q>(D, pq + s + o, l, q);
+                    if (vm & 2u) st_one<S, Q>(D, pq + s + 1 + o, h, q);
+                }
             } else {
+                const bool bl = (m_lo >> L::opp(q)) & 1u, bh = (m_hi >> L::opp(q)) & 1u;
+                const uint32_t po = (uint32_t)L::opp(q) * st;
                 float l, h;
                 f2split(v, l, h);
                 if (bl && !bounce_back_pop<Q>(L::opp(q), wm & 1u, a.corr)) l = 0.f;

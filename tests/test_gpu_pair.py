@@ -246,3 +246,28 @@ def test_pattern_conversion_keeps_results(precision):
     with pytest.raises(_capi.LbmError) as e:
         b.set_pattern("pull")        # after an odd launch: not a pull state
     assert e.value.status == _capi.ERR_STATE
+
+
+@pytest.mark.parametrize("corrections", [0, _capi.FIX_BB_ALL_DIRS | _capi.FIX_LIST_NODES])
+@pytest.mark.parametrize("precision", ["f16s", "bf16s"])
+def test_pair_kernel_16bit_aa_matches_single_kernel(precision, corrections):
+    """16-bit AA storage: the paired kernel's bounce-back, initial values and
+    ghost-slot handling against the one-node-per-lane kernel on a tortuous
+    vessel with walls, inlet and outlet nodes.  Both compute in FP32 (in a
+    different order) and round to the same storage, so the deviations f - w
+    agree to a few storage roundings; a wrong bounced or initial value at the
+    boundary nodes moves their relative L2 difference above 1e-2."""
+    c = cases.vessel(4003)
+    geom = c.geometry()
+    out = {}
+    for npl in (1, 2):
+        sim = Simulation(geom, c.tau, c.boundary_specs(geom), precision=precision, pattern="aa",
+                         nodes_per_lane=npl, staging=1, corrections=corrections)
+        sim.step(9)
+        out[npl] = sim.fields()
+    from pv2013_gb300.engine import LatticeModel
+    w = LatticeModel(19).w
+    d1, d2 = out[1][0] - w, out[2][0] - w
+    assert np.isfinite(d2).all()
+    assert rel_l2(d2, d1) < (2e-3 if precision == "f16s" else 2e-2)
+    assert rel_l2(out[2][2], out[1][2]) < (2e-3 if precision == "f16s" else 2e-2)
