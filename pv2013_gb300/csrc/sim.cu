@@ -1379,7 +1379,6 @@ static lbm_status convert_pattern(lbm_sim* S, int pattern, cudaStream_t st) {
         return LBM_OK;
     };
     if (pattern == LBM_PULL) {
-        if (S->npl == 4) return fail(LBM_ERR_ARG, "the four-level kernel runs the AA pattern only");
         if (aa_mode(S) != MODE_AA_ODD)
             return fail(LBM_ERR_STATE, "AA -> pull needs the state after an even (node-local) launch; step once more");
         if (!S->buf[1] && cudaMalloc(&S->buf[1], bytes) != cudaSuccess) {
@@ -1424,7 +1423,7 @@ lbm_status lbm_sim_autotune(lbm_sim* S, int32_t launches, void* stream, lbm_tune
     // patterns: the current one; the other one where the state converts now
     // (AA -> pull after an even launch; pull -> AA always) and its memory fits
     std::vector<int> patterns = {S->pattern};
-    if (S->npl != 4 && (S->pattern == LBM_PULL || aa_mode(S) == MODE_AA_ODD))
+    if (S->pattern == LBM_PULL || aa_mode(S) == MODE_AA_ODD)
         patterns.push_back(S->pattern == LBM_PULL ? LBM_AA : LBM_PULL);
     void* scratch[2] = {nullptr, nullptr};
     const bool need2 = std::find(patterns.begin(), patterns.end(), (int)LBM_PULL) != patterns.end();
@@ -1443,11 +1442,6 @@ lbm_status lbm_sim_autotune(lbm_sim* S, int32_t launches, void* stream, lbm_tune
     std::vector<Cand> cands;
     const int wpbs[4] = {1, 2, 4, 8};
     for (int pat : patterns) {
-        if (S->npl == 4) {
-            // the four-level lattice and its state layout serve the four-level kernel only
-            for (int w : wpbs) cands.push_back({pat, 4, 1, w, S->piece, 0.f});
-            continue;
-        }
         for (int w : wpbs) cands.push_back({pat, 1, 1, w, S->piece, 0.f});
         for (int w : wpbs) cands.push_back({pat, 1, 0, w, S->piece, 0.f});
         if (S->store != ST_F64)
@@ -1495,7 +1489,7 @@ lbm_status lbm_sim_autotune(lbm_sim* S, int32_t launches, void* stream, lbm_tune
     if (e1) cudaEventDestroy(e1);
     for (void* b : scratch) if (b) cudaFree(b);
     S->pattern = save_pattern; S->npl = save_npl; S->staging = save_staging; S->wpb = save_wpb;
-    if (S->npl != 4) select_piece(S, save_piece);
+    select_piece(S, save_piece);
     if (res != LBM_OK) return res;
     LBM_TRY(check_timeout(S, st));
     const Cand* best = &cands[0];

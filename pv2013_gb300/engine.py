@@ -393,11 +393,11 @@ class Simulation:
         size, streaming pattern) on scratch copies of the state and keeps the
         fastest; returns [(nodes_per_lane, staging, warps_per_block,
         ms_per_launch, chosen, pattern, piece_slots)]."""
-        ents = (_capi.TuneEntry * 64)()
+        ents = (_capi.TuneEntry * 128)()
         n = C.c_size_t()
-        check(load().lbm_sim_autotune(self._h, int(launches), self._stream, ents, 64, C.byref(n)))
+        check(load().lbm_sim_autotune(self._h, int(launches), self._stream, ents, 128, C.byref(n)))
         return [(e.nodes_per_lane, e.staging, e.warps_per_block, e.ms_per_launch, bool(e.chosen),
-                 {_capi.PULL: "pull", _capi.AA: "aa"}[e.pattern], e.piece_slots) for e in ents[:min(n.value, 64)]]
+                 {_capi.PULL: "pull", _capi.AA: "aa"}[e.pattern], e.piece_slots) for e in ents[:min(n.value, 128)]]
 
     def set_pattern(self, pattern):
         """Converts the state to another streaming pattern ("pull" or "aa")."""
