@@ -349,7 +349,8 @@ def gpu_arm(args, rank, world):
     torch.cuda.synchronize()
     t4 = time.time()
     e2e_sec = t4 - t0
-    e2e_parts = {"geometry_s": t1 - t0, "lattice_build_s": t2 - t1, "steps_s": t3 - t2, "fields_d2h_s": t4 - t3}
+    e2e_parts = {"geometry_s": t1 - t0, "lattice_build_s": t2 - t1, "steps_s": t3 - t2, "fields_d2h_s": t4 - t3,
+                 "geometry_voxelize_ms": g2.info.voxelize_ms, "geometry_classify_ms": g2.info.classify_ms}
     e2e_mlups = nf * e2e_steps / e2e_sec / 1e6 * world
     del s2, g2
     h2d = case.triangles.nbytes + 8 * len(case.inlet_profile(geom)) + 8 * len(case.amp_table())

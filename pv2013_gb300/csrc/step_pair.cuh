@@ -307,7 +307,7 @@ __global__ void __launch_bounds__(256) __maxnreg__((PairMaxReg<Q, S, MODE>::valu
     // population windows are prefetched into L2 below (the load is in flight
     // with d0)
     const int64_t cfp = ci + a.pf_ahead;
-    const bool hfp = a.pf_ahead > 0 && cfp < a.nchunks;
+    const bool hfp = MODE != MODE_AA_ODD && a.pf_ahead > 0 && cfp < a.nchunks;   // (the odd launch: none)
     uint32_t nfp = 0;
     if (hfp) asm volatile("ld.global.nc.u32 %0, [%1];" : "=r"(nfp) : "l"(&a.chunks[cfp].n0));
     const uint4 d1 = have_chunk ? __ldg(cw + 1) : make_uint4(0u, 0u, 0u, 0u);
@@ -587,9 +587,12 @@ static lbm_status launch_pair_one(const StepArgs& a, int wpb, cudaStream_t st) {
             return fail(LBM_ERR_CUDA, "paired step kernel occupancy: %s", cudaGetErrorString(cudaGetLastError()));
         resident[dev][wpb] = sms * (nb > 0 ? nb : 1);
     }
-    // half a wave ahead: measured 0.4 % faster than one wave, 1.5 % faster than 1.5 waves
+    // half a wave ahead: measured 0.4 % faster than one wave, 1.5 % faster
+    // than 1.5 waves.  The AA odd launch prefetches nothing: on its grouped
+    // piece table the prefetch cost more than it saved (without it the
+    // tree's step measured 2.7 % faster; one or two waves ahead: no gain)
     StepArgs b = a;
-    b.pf_ahead = (int64_t)resident[dev][wpb] * per_block / 2;
+    b.pf_ahead = MODE == MODE_AA_ODD ? 0 : (int64_t)resident[dev][wpb] * per_block / 2;
     k_step2<Q, S, MODE, RA><<<(unsigned)(blocks > 0 ? blocks : 1), 32 * wpb, smem, st>>>(b);
     return LBM_OK;
 }
