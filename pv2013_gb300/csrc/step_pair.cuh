@@ -404,6 +404,10 @@ __global__ void __launch_bounds__(256) __maxnreg__((PairMaxReg<Q, S, MODE>::valu
         for (int q = t; q < Q; q += 1 << lg)
             asm volatile("prefetch.global.L2 [%0];" ::"l"(Ab + (size_t)((uint32_t)q * sw + wf) * sizeof(W)));
     }
+    // the AA odd launch prefetches only the descriptor of the piece a wave
+    // ahead (its population windows: see the launcher)
+    if (MODE == MODE_AA_ODD && t == 0 && a.pf_ahead > 0 && cfp < a.nchunks)
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(a.chunks + cfp));
     // the odd pattern's column bases go through shared memory (lane 0 of
     // each chunk wrote them): fewer registers held across the collision
     if constexpr (MODE == MODE_AA_ODD) __syncwarp();
@@ -588,11 +592,13 @@ static lbm_status launch_pair_one(const StepArgs& a, int wpb, cudaStream_t st) {
         resident[dev][wpb] = sms * (nb > 0 ? nb : 1);
     }
     // half a wave ahead: measured 0.4 % faster than one wave, 1.5 % faster
-    // than 1.5 waves.  The AA odd launch prefetches nothing: on its grouped
-    // piece table the prefetch cost more than it saved (without it the
-    // tree's step measured 2.7 % faster; one or two waves ahead: no gain)
+    // than 1.5 waves.  The AA odd launch prefetches no population window: on
+    // its grouped piece table that cost more than it saved (without it the
+    // tree's step measured 2.7 % faster; one or two waves ahead: no gain);
+    // it prefetches the descriptor one wave ahead (+1 %; half a wave and two
+    // waves measured the same within 0.3 %)
     StepArgs b = a;
-    b.pf_ahead = MODE == MODE_AA_ODD ? 0 : (int64_t)resident[dev][wpb] * per_block / 2;
+    b.pf_ahead = (int64_t)resident[dev][wpb] * per_block / (MODE == MODE_AA_ODD ? 1 : 2);
     k_step2<Q, S, MODE, RA><<<(unsigned)(blocks > 0 ? blocks : 1), 32 * wpb, smem, st>>>(b);
     return LBM_OK;
 }
