@@ -158,6 +158,7 @@ struct StepArgs {
     uint32_t corr;            // lbm_sim_params.corrections (LBM_FIX_* bits)
     int32_t piece_lg;         // paired kernel: log2 of the lanes per chunk piece (2, 3 or 4)
     int64_t pf_ahead;         // paired kernel: L2 prefetch distance in chunk pieces (0 = none)
+    const uint2* even_desc;   // paired kernel, AA even launch: per piece (n0, len_inst | 64 if a Zou-He lane)
     uint32_t spin_limit;      // TMA-staged kernel: polls of a stage's mbarrier before giving up (0 = default)
     int32_t stall_first;      // TMA-staged kernel, failure tests: each warp's first stage is never issued
 };

@@ -475,6 +475,17 @@ __global__ void __launch_bounds__(kGroupMax) k_group_pieces(const Chunk* __restr
     }
 }
 
+// The AA even launch's 8-byte piece records: (n0, len_inst), bit 6 of
+// len_inst set when the piece has a Zou-He lane (the launch then reads the
+// descriptor's zmask); everything else of the 64-byte descriptor serves the
+// neighbour launches only.
+__global__ void k_even_desc(const Chunk* __restrict__ c, int64_t n, uint2* __restrict__ out) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const Chunk& ch = c[i];
+        out[i] = make_uint2((uint32_t)ch.n0, (ch.len_inst & ~0xc0u) | (ch.zmask ? 64u : 0u));
+    }
+}
+
 template <class T>
 __global__ void k_init_pop(T* __restrict__ a, int64_t stride, int Q, const double* __restrict__ val) {
     const int64_t n = stride * Q;
@@ -558,6 +569,8 @@ struct lbm_sim {
     Chunk* chunks2s[3] = {nullptr, nullptr, nullptr};   // paired tables of 8-, 16- and 32-slot pieces
     Chunk* chunks2g = nullptr;     // the same pieces grouped (k_group_pieces): the AA odd launch's table
     Chunk* chunks2gs[3] = {nullptr, nullptr, nullptr};
+    uint2* even2 = nullptr;        // the AA even launch's 8-byte records of chunks2 (k_even_desc)
+    uint2* even2s[3] = {nullptr, nullptr, nullptr};
     int64_t nchunks2s[3] = {0, 0, 0};
     int aa_phase = 0;              // AA: launch n is an even (node-local) launch when n + aa_phase is even
     ZSlot* zslots = nullptr;
@@ -830,7 +843,7 @@ lbm_status build_instance(const lbm_geometry* g, const lbm_sim_params* p, int Q,
 
 lbm_status sim_launch(lbm_sim* S, int mode, bool dry, void* src, void* dst, int64_t step, const int64_t* step_base,
                       const Partials& part, double* of, double* orho, double* ou, cudaStream_t st) {
-    StepArgs a;
+    StepArgs a{};
     a.chunks = S->chunks; a.nchunks = S->nchunks;
     a.src = src; a.dst = dst; a.stride = S->stride;
     a.zslots = S->zslots; a.lists = S->lists; a.insts = S->insts; a.amp = S->amp;
@@ -844,6 +857,7 @@ lbm_status sim_launch(lbm_sim* S, int mode, bool dry, void* src, void* dst, int6
     if (!dry && S->npl == 2) {
         a.chunks = mode == MODE_AA_ODD ? S->chunks2g : S->chunks2;
         a.nchunks = S->nchunks2;
+        a.even_desc = S->even2;
         switch (S->store) {
             case ST_F32: return launch_pair_f32(S->Q, mode, S->ra, a, S->wpb, st);
             case ST_F16S: return launch_pair_f16s(S->Q, mode, S->ra, a, S->wpb, st);
@@ -896,6 +910,7 @@ void select_piece(lbm_sim* S, int piece) {
     S->piece = piece;
     S->chunks2 = S->chunks2s[k];
     S->chunks2g = S->chunks2gs[k];
+    S->even2 = S->even2s[k];
     S->nchunks2 = S->nchunks2s[k];
 }
 
@@ -1105,6 +1120,12 @@ lbm_status sim_create(const lbm_geometry* const* g, const lbm_sim_params* p, siz
         const int64_t nwin = (nch2[k] + win - 1) / win;
         k_group_pieces<<<(unsigned)std::min<int64_t>(nwin, 152 * 8), kGroupMax, 0, st>>>(S->chunks2s[k],
                                                                                           S->chunks2gs[k], nch2[k], win);
+        LBM_CUDA(cudaGetLastError());
+    }
+    for (int k = 0; k < 3 && S->store != ST_F64; ++k) {
+        LBM_CUDA(cudaMalloc(&S->even2s[k], sizeof(uint2) * std::max<int64_t>(nch2[k], 1)));
+        if (nch2[k] == 0) continue;
+        k_even_desc<<<blocks_for(nch2[k], 256), 256, 0, st>>>(S->chunks2s[k], nch2[k], S->even2s[k]);
         LBM_CUDA(cudaGetLastError());
     }
     select_piece(S.get(), S->piece);       // after the piece tables exist
@@ -1940,6 +1961,7 @@ void lbm_sim_destroy(lbm_sim* S) {
     if (S->chunks) cudaFree(S->chunks);
     for (Chunk* c : S->chunks2s) if (c) cudaFree(c);
     for (Chunk* c : S->chunks2gs) if (c) cudaFree(c);
+    for (uint2* c : S->even2s) if (c) cudaFree(c);
     if (S->wall_pos) cudaFree(S->wall_pos);
     if (S->zslots) cudaFree(S->zslots);
     if (S->lists) cudaFree(S->lists);

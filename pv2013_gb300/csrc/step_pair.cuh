@@ -300,23 +300,38 @@ __global__ void __launch_bounds__(256) __maxnreg__((PairMaxReg<Q, S, MODE>::valu
     const int pw = lane >> lg;                    // piece of this lane within the warp
     const int64_t ci = (((int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) << (5 - lg)) + pw;
     const bool have_chunk = ci < a.nchunks;
-    // chunk descriptor words 0-7 (n0, len_inst, wmask, zmask, bmask, zslot0, mslot0, K0)
+    // chunk descriptor words 0-7 (n0, len_inst, wmask, zmask, bmask, zslot0, mslot0, K0);
+    // the AA even launch reads the 8-byte record (n0, len_inst) instead and
+    // the descriptor's zmask only for pieces with a Zou-He lane
     const uint4* cw = reinterpret_cast<const uint4*>(a.chunks + (have_chunk ? ci : 0));
-    const uint4 d0 = have_chunk ? __ldg(cw) : make_uint4(0u, 0u, 0u, 0u);
+    uint4 d0;
+    if constexpr (MODE == MODE_AA_EVEN) {
+        const uint2 de = have_chunk ? __ldg(a.even_desc + ci) : make_uint2(0u, 0u);
+        d0 = make_uint4(de.x, de.y, 0u, 0u);
+    } else {
+        d0 = have_chunk ? __ldg(cw) : make_uint4(0u, 0u, 0u, 0u);
+    }
     // start id of the piece half a wave of resident warps ahead: its
     // population windows are prefetched into L2 below (the load is in flight
     // with d0)
     const int64_t cfp = ci + a.pf_ahead;
     const bool hfp = MODE != MODE_AA_ODD && a.pf_ahead > 0 && cfp < a.nchunks;   // (the odd launch: none)
     uint32_t nfp = 0;
-    if (hfp) asm volatile("ld.global.nc.u32 %0, [%1];" : "=r"(nfp) : "l"(&a.chunks[cfp].n0));
-    const uint4 d1 = have_chunk ? __ldg(cw + 1) : make_uint4(0u, 0u, 0u, 0u);
+    if (hfp) {
+        if constexpr (MODE == MODE_AA_EVEN)
+            asm volatile("ld.global.nc.u32 %0, [%1];" : "=r"(nfp) : "l"(&a.even_desc[cfp].x));
+        else
+            asm volatile("ld.global.nc.u32 %0, [%1];" : "=r"(nfp) : "l"(&a.chunks[cfp].n0));
+    }
+    const uint4 d1 = have_chunk && MODE != MODE_AA_EVEN ? __ldg(cw + 1) : make_uint4(0u, 0u, 0u, 0u);
     const int32_t n0 = (int32_t)d0.x;
     const uint32_t li = d0.y;
     const bool act = have_chunk && 2 * t < (int)(li & 63u);
     // node slots 2t (lo) and 2t+1 (hi) of the chunk
     const uint32_t bm_all = act ? d1.x : 0u;
-    const uint32_t zm_all = act ? d0.w : 0u;
+    uint32_t zm_all = act ? d0.w : 0u;
+    if (MODE == MODE_AA_EVEN && act && (li & 64u))
+        asm volatile("ld.global.nc.u32 %0, [%1];" : "=r"(zm_all) : "l"(&cw[0].w));   // zmask
     uint32_t m_lo = 0u, m_hi = 0u;
     if (MODE != MODE_AA_EVEN && ((bm_all >> (2 * t)) & 3u)) {
         const int32_t ms = (int32_t)d1.z + __popc(bm_all & ((1u << (2 * t)) - 1u));
