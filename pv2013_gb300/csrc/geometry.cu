@@ -391,16 +391,18 @@ static int g_blocks_for(int64_t n, int threads) {
     return (int)b;
 }
 
-// Device buffer that frees itself.
+// Device buffer that frees itself, from the device's stream-ordered pool
+// (dev_alloc): allocated and freed in the order of the stream that uses it.
 template <class T>
 struct DBuf {
     T* p = nullptr;
-    ~DBuf() { if (p) cudaFree(p); }
-    lbm_status alloc(size_t n, const char* what) {
-        if (cudaMalloc(&p, sizeof(T) * (n ? n : 1)) != cudaSuccess)
-            return fail(LBM_ERR_NOMEM, "cudaMalloc for %s (%zu elements) failed", what, n);
-        return LBM_OK;
+    cudaStream_t s = 0;
+    ~DBuf() { if (p) dev_free(p, s); }
+    lbm_status alloc(size_t n, const char* what, cudaStream_t st) {
+        s = st;
+        return dev_alloc(reinterpret_cast<void**>(&p), sizeof(T) * (n ? n : 1), st, what);
     }
+    void adopt(T* q, cudaStream_t st) { p = q; s = st; }
     T* release() { T* q = p; p = nullptr; return q; }
 };
 
@@ -459,17 +461,17 @@ static lbm_status geometry_build(lbm_geometry* G, const lbm_tri* tris, size_t nt
     LBM_CUDA(cudaEventCreate(&e2));
 
     DBuf<double> d_tris;
-    LBM_TRY(d_tris.alloc(ntris * 12, "triangles"));
+    LBM_TRY(d_tris.alloc(ntris * 12, "triangles", st));
     if (ntris) LBM_CUDA(cudaMemcpyAsync(d_tris.p, tris, sizeof(double) * 12 * ntris, cudaMemcpyHostToDevice, st));
     DBuf<int32_t> colcount, cursor, glist, nglob;
     DBuf<int64_t> colstart;
     DBuf<uint8_t> flags;
-    LBM_TRY(colcount.alloc(ncol, "column counts"));
-    LBM_TRY(cursor.alloc(ncol, "column cursors"));
-    LBM_TRY(colstart.alloc(ncol + 1, "column offsets"));
-    LBM_TRY(glist.alloc(ntris, "global triangle list"));
-    LBM_TRY(nglob.alloc(1, "global count"));
-    LBM_TRY(flags.alloc(npts, "node-type field"));
+    LBM_TRY(colcount.alloc(ncol, "column counts", st));
+    LBM_TRY(cursor.alloc(ncol, "column cursors", st));
+    LBM_TRY(colstart.alloc(ncol + 1, "column offsets", st));
+    LBM_TRY(glist.alloc(ntris, "global triangle list", st));
+    LBM_TRY(nglob.alloc(1, "global count", st));
+    LBM_TRY(flags.alloc(npts, "node-type field", st));
     LBM_CUDA(cudaEventRecord(e0, st));
     LBM_CUDA(cudaMemsetAsync(colcount.p, 0, sizeof(int32_t) * ncol, st));
     LBM_CUDA(cudaMemsetAsync(cursor.p, 0, sizeof(int32_t) * ncol, st));
@@ -482,7 +484,7 @@ static lbm_status geometry_build(lbm_geometry* G, const lbm_tri* tris, size_t nt
     int32_t nglobal = 0;
     LBM_CUDA(cudaMemcpyAsync(&nglobal, nglob.p, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
     DBuf<int32_t> pairs;
-    LBM_TRY(pairs.alloc(npairs, "column candidate lists"));
+    LBM_TRY(pairs.alloc(npairs, "column candidate lists", st));
     if (ntris) k_tri_fill<<<(unsigned)((ntris + TB - 1) / TB), TB, 0, st>>>(g, d_tris.p, (int64_t)ntris, colstart.p, cursor.p, pairs.p);
     LBM_CUDA(cudaStreamSynchronize(st));
     k_columns<<<(unsigned)((ncol + kVoxWarps - 1) / kVoxWarps), kVoxWarps * 32, 0, st>>>(
@@ -492,14 +494,14 @@ static lbm_status geometry_build(lbm_geometry* G, const lbm_tri* tris, size_t nt
 
     // boundary points and predicate lists
     DBuf<uint8_t> isb;
-    LBM_TRY(isb.alloc(npts, "boundary flags"));
+    LBM_TRY(isb.alloc(npts, "boundary flags", st));
     k_boundary<<<g_blocks_for(npts, 256), 256, 0, st>>>(g, flags.p, isb.p);
     LBM_TRY(scan::count_nonzero(flags.p, npts, &G->n_fluid, st));
     int64_t* bidx = nullptr;
     LBM_TRY(scan::compact(isb.p, npts, &bidx, &G->n_boundary, st));
     G->d_bidx = bidx;
     DBuf<uint64_t> bmask;
-    LBM_TRY(bmask.alloc(G->n_boundary, "boundary masks"));
+    LBM_TRY(bmask.alloc(G->n_boundary, "boundary masks", st));
     std::vector<DevPred> hp(npreds);
     int32_t nl = 0;
     for (size_t p = 0; p < npreds; ++p) {
@@ -508,7 +510,7 @@ static lbm_status geometry_build(lbm_geometry* G, const lbm_tri* tris, size_t nt
         nl = std::max(nl, preds[p].list_id + 1);
     }
     DBuf<DevPred> dpred;
-    LBM_TRY(dpred.alloc(npreds, "predicates"));
+    LBM_TRY(dpred.alloc(npreds, "predicates", st));
     if (npreds) LBM_CUDA(cudaMemcpyAsync(dpred.p, hp.data(), sizeof(DevPred) * npreds, cudaMemcpyHostToDevice, st));
     if (G->n_boundary)
         k_predicates<<<g_blocks_for(G->n_boundary, 256), 256, 0, st>>>(g, bidx, G->n_boundary, dpred.p, (int)npreds, bmask.p);
@@ -520,7 +522,7 @@ static lbm_status geometry_build(lbm_geometry* G, const lbm_tri* tris, size_t nt
     G->list_sizes.assign(64, 0);
     {
         DBuf<uint8_t> fl;
-        LBM_TRY(fl.alloc(G->n_boundary, "list flags"));
+        LBM_TRY(fl.alloc(G->n_boundary, "list flags", st));
         for (int l = -1; l < nl; ++l) {
             k_list_flag<<<g_blocks_for(G->n_boundary, 256), 256, 0, st>>>(G->d_bmask, G->n_boundary, l, fl.p);
             int64_t c = 0;
@@ -625,15 +627,15 @@ lbm_status lbm_geometry_list(const lbm_geometry* G, int32_t list, int64_t* host_
     }
     cudaStream_t st = 0;
     DBuf<uint8_t> fl;
-    LBM_TRY(fl.alloc(G->n_boundary, "list flags"));
+    LBM_TRY(fl.alloc(G->n_boundary, "list flags", st));
     k_list_flag<<<g_blocks_for(G->n_boundary, 256), 256, 0, st>>>(G->d_bmask, G->n_boundary,
                                                                   list == LBM_LIST_WALL ? -1 : list, fl.p);
     int64_t* pos = nullptr;
     int64_t c = 0;
     LBM_TRY(scan::compact(fl.p, G->n_boundary, &pos, &c, st));
-    DBuf<int64_t> posb; posb.p = pos;
+    DBuf<int64_t> posb; posb.adopt(pos, st);
     DBuf<int64_t> vals;
-    LBM_TRY(vals.alloc(c, "list values"));
+    LBM_TRY(vals.alloc(c, "list values", st));
     k_gather_i64<<<g_blocks_for(c, 256), 256, 0, st>>>(G->d_bidx, pos, c, vals.p);
     LBM_CUDA(cudaMemcpy(host_out, vals.p, sizeof(int64_t) * c, cudaMemcpyDeviceToHost));
     return LBM_OK;
@@ -641,6 +643,7 @@ lbm_status lbm_geometry_list(const lbm_geometry* G, int32_t list, int64_t* host_
 
 void lbm_geometry_destroy(lbm_geometry* G) {
     if (!G) return;
+    cudaDeviceSynchronize();               // pool memory is freed without an implicit wait
     if (G->d_flags) cudaFree(G->d_flags);
     if (G->d_bidx) cudaFree(G->d_bidx);
     if (G->d_bmask) cudaFree(G->d_bmask);

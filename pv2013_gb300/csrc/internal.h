@@ -15,6 +15,14 @@ namespace lbm {
 lbm_status fail(lbm_status s, const char* fmt, ...);
 void clear_error();
 
+// Temporary device memory from the device's stream-ordered pool, allocated
+// and freed in the order of `stream` (a cudaStream_t).  The pool keeps up to
+// a few GB between uses, so a lattice or geometry build does not go back to
+// the driver for every scratch array.  cudaFree of such memory does not wait
+// for the device: callers synchronise first.
+lbm_status dev_alloc(void** p, size_t bytes, void* stream, const char* what);
+void dev_free(void* p, void* stream);
+
 // Triangle array helpers (host).
 using TriVec = std::vector<lbm_tri>;
 lbm_status to_c_array(const TriVec& v, lbm_tri** out, size_t* n);

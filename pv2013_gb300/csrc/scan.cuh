@@ -124,18 +124,25 @@ struct Workspace {
     int64_t* tiles = nullptr;
     int64_t* total = nullptr;
     int64_t ntiles = 0;
+    cudaStream_t st = 0;
 };
 
-inline lbm_status ws_alloc(Workspace& w, int64_t n) {
+#define LBM_SCAN_TRY(x)                 \
+    do {                                \
+        lbm_status s_ = (x);            \
+        if (s_ != LBM_OK) return s_;    \
+    } while (0)
+
+inline lbm_status ws_alloc(Workspace& w, int64_t n, cudaStream_t st) {
     w.ntiles = (n + kTile - 1) / kTile;
     if (w.ntiles < 1) w.ntiles = 1;
-    if (cudaMalloc(&w.tiles, sizeof(int64_t) * (w.ntiles + 1)) != cudaSuccess)
-        return fail(LBM_ERR_NOMEM, "scan workspace: cudaMalloc of %lld tiles failed", (long long)w.ntiles);
+    LBM_SCAN_TRY(dev_alloc(reinterpret_cast<void**>(&w.tiles), sizeof(int64_t) * (w.ntiles + 1), st, "scan workspace"));
     w.total = w.tiles + w.ntiles;
+    w.st = st;
     return LBM_OK;
 }
 inline void ws_free(Workspace& w) {
-    if (w.tiles) cudaFree(w.tiles);
+    if (w.tiles) dev_free(w.tiles, w.st);
     w.tiles = nullptr;
 }
 
@@ -143,7 +150,7 @@ inline void ws_free(Workspace& w) {
 template <class T>
 lbm_status exclusive_scan(const T* d_in, int64_t n, int64_t* d_out, int64_t* h_total, cudaStream_t st) {
     Workspace w;
-    lbm_status s = ws_alloc(w, n);
+    lbm_status s = ws_alloc(w, n, st);
     if (s != LBM_OK) return s;
     tile_totals<T><<<(unsigned)w.ntiles, kThreads, 0, st>>>(d_in, n, w.tiles, false);
     scan_totals<<<1, kThreads, 0, st>>>(w.tiles, w.ntiles, w.total);
@@ -159,7 +166,7 @@ lbm_status exclusive_scan(const T* d_in, int64_t n, int64_t* d_out, int64_t* h_t
 template <class T>
 lbm_status count_nonzero(const T* d_in, int64_t n, int64_t* h_count, cudaStream_t st) {
     Workspace w;
-    lbm_status s = ws_alloc(w, n);
+    lbm_status s = ws_alloc(w, n, st);
     if (s != LBM_OK) return s;
     tile_totals<T><<<(unsigned)w.ntiles, kThreads, 0, st>>>(d_in, n, w.tiles, true);
     scan_totals<<<1, kThreads, 0, st>>>(w.tiles, w.ntiles, w.total);
@@ -170,19 +177,20 @@ lbm_status count_nonzero(const T* d_in, int64_t n, int64_t* h_count, cudaStream_
     return LBM_OK;
 }
 
-// Ordered indices of nonzero entries into *d_out (allocated here, count in *h_count).
+// Ordered indices of nonzero entries into *d_out (allocated here from the
+// stream-ordered pool on st, count in *h_count).
 template <class T>
 lbm_status compact(const T* d_in, int64_t n, int64_t** d_out, int64_t* h_count, cudaStream_t st) {
     Workspace w;
-    lbm_status s = ws_alloc(w, n);
+    lbm_status s = ws_alloc(w, n, st);
     if (s != LBM_OK) return s;
     tile_totals<T><<<(unsigned)w.ntiles, kThreads, 0, st>>>(d_in, n, w.tiles, true);
     scan_totals<<<1, kThreads, 0, st>>>(w.tiles, w.ntiles, w.total);
     cudaError_t e = cudaMemcpyAsync(h_count, w.total, sizeof(int64_t), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) { ws_free(w); return fail(LBM_ERR_CUDA, "compact: %s", cudaGetErrorString(e)); }
-    e = cudaMalloc(d_out, sizeof(int64_t) * (*h_count > 0 ? *h_count : 1));
-    if (e != cudaSuccess) { ws_free(w); return fail(LBM_ERR_NOMEM, "compact: cudaMalloc of %lld indices", (long long)*h_count); }
+    s = dev_alloc(reinterpret_cast<void**>(d_out), sizeof(int64_t) * (*h_count > 0 ? *h_count : 1), st, "compacted indices");
+    if (s != LBM_OK) { ws_free(w); return s; }
     tile_compact_write<T><<<(unsigned)w.ntiles, kThreads, 0, st>>>(d_in, n, w.tiles, *d_out);
     e = cudaStreamSynchronize(st);
     ws_free(w);

@@ -48,6 +48,44 @@ using namespace lbm;
 
 extern "C" void lbm_sim_destroy(lbm_sim* S);
 
+namespace lbm {
+
+// The pool keeps this much memory between frees and allocations (default
+// pools of this process only; nothing outlives the process).
+static constexpr uint64_t kPoolKeepBytes = 8ull << 30;
+
+lbm_status dev_alloc(void** p, size_t bytes, void* stream, const char* what) {
+    static std::mutex mu;
+    static bool tuned[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64) {
+        std::lock_guard<std::mutex> lock(mu);
+        if (!tuned[dev]) {
+            cudaMemPool_t pool;
+            if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+                uint64_t keep = kPoolKeepBytes;
+                cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+            }
+            cudaGetLastError();
+            tuned[dev] = true;
+        }
+    }
+    *p = nullptr;
+    const cudaError_t e = cudaMallocAsync(p, bytes, (cudaStream_t)stream);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        return fail(LBM_ERR_NOMEM, "device allocation for %s (%zu bytes) failed: %s", what, bytes, cudaGetErrorString(e));
+    }
+    return LBM_OK;
+}
+
+void dev_free(void* p, void* stream) {
+    if (p) cudaFreeAsync(p, (cudaStream_t)stream);
+}
+
+}  // namespace lbm
+
 #define LBM_TRY(x)                      \
     do {                                \
         lbm_status s_ = (x);            \
@@ -56,18 +94,22 @@ extern "C" void lbm_sim_destroy(lbm_sim* S);
 
 namespace {
 
+// Device buffer that frees itself, from the device's stream-ordered pool
+// (dev_alloc): allocated and freed in the order of the stream that uses it.
 template <class T>
 struct DBuf {
     T* p = nullptr;
+    cudaStream_t s = 0;
     DBuf() = default;
     DBuf(const DBuf&) = delete;
-    ~DBuf() { if (p) cudaFree(p); }
-    lbm_status alloc(size_t n, const char* what) {
-        if (p) { cudaFree(p); p = nullptr; }
-        if (cudaMalloc(&p, sizeof(T) * (n ? n : 1)) != cudaSuccess)
-            return fail(LBM_ERR_NOMEM, "cudaMalloc for %s (%zu elements) failed", what, n);
-        return LBM_OK;
+    ~DBuf() { if (p) dev_free(p, s); }
+    lbm_status alloc(size_t n, const char* what, cudaStream_t st) {
+        if (p) { dev_free(p, s); p = nullptr; }
+        s = st;
+        return dev_alloc(reinterpret_cast<void**>(&p), sizeof(T) * (n ? n : 1), st, what);
     }
+    // takes ownership of pool memory allocated on stream st
+    void adopt(T* q, cudaStream_t st) { p = q; s = st; }
     T* release() { T* q = p; p = nullptr; return q; }
 };
 
@@ -166,7 +208,7 @@ __global__ void k_dil_a(const uint8_t* __restrict__ t2, const uint8_t* __restric
 // byte per cell
 lbm_status compute_types(const uint8_t* pflags, const Pad& D, uint8_t* type, cudaStream_t st) {
     DBuf<uint8_t> tmp;
-    LBM_TRY(tmp.alloc(D.cells(), "node type scratch"));
+    LBM_TRY(tmp.alloc(D.cells(), "node type scratch", st));
     const dim3 grid((unsigned)((D.Pr() + 255) / 256), (unsigned)D.Pb(), (unsigned)D.Pa());
     k_dil_r<<<grid, 256, 0, st>>>(pflags, D, type);
     k_dil_b<<<grid, 256, 0, st>>>(type, D, tmp.p);
@@ -668,7 +710,7 @@ lbm_status count_chunks(const lbm_geometry* g, int ra, int piece, bool pairs, cu
     int dims[3];
     geometry_dims(g, dims);
     DBuf<unsigned long long> tot;
-    LBM_TRY(tot.alloc(1, "chunk count"));
+    LBM_TRY(tot.alloc(1, "chunk count", st));
     LBM_CUDA(cudaMemsetAsync(tot.p, 0, sizeof(unsigned long long), st));
     const int64_t ncol = (int64_t)dims[0] * (ra == 2 ? dims[1] : dims[2]);
     k_count_runs<<<blocks_for(ncol, 128), 128, 0, st>>>(geometry_flags_dev(g), dims[0], dims[1], dims[2], ra, piece,
@@ -692,39 +734,39 @@ lbm_status build_instance(const lbm_geometry* g, const lbm_sim_params* p, int Q,
     DBuf<uint8_t> fperm;
     const uint8_t* pflags = flags;
     if (ra != 2) {
-        LBM_TRY(fperm.alloc(npts, "permuted flags"));
+        LBM_TRY(fperm.alloc(npts, "permuted flags", st));
         k_permute_flags<<<blocks_for(npts, 256), 256, 0, st>>>(flags, P, fperm.p);
         pflags = fperm.p;
     }
     // 1. fluid + ghost nodes on the padded grid, numbered in permuted order
     const Pad D{P.Na(), P.Nb(), P.Nr()};
     DBuf<uint8_t> type;
-    LBM_TRY(type.alloc(D.cells(), "node types"));
+    LBM_TRY(type.alloc(D.cells(), "node types", st));
     LBM_TRY(compute_types(pflags, D, type.p, st));
     k_parity_ghosts<<<blocks_for(D.cells(), 256), 256, 0, st>>>(D, type.p);
     int64_t* nc = nullptr;
     LBM_TRY(scan::compact(type.p, D.cells(), &nc, &out.N, st));
-    DBuf<int64_t> node_cell; node_cell.p = nc;
+    DBuf<int64_t> node_cell; node_cell.adopt(nc, st);
     if (node_off + out.N >= INT32_MAX) return fail(LBM_ERR_ARG, "more than 2^31 lattice nodes");
     DBuf<int32_t> noc;
-    LBM_TRY(noc.alloc(D.cells(), "node map"));
+    LBM_TRY(noc.alloc(D.cells(), "node map", st));
     LBM_CUDA(cudaMemsetAsync(noc.p, 0xff, sizeof(int32_t) * D.cells(), st));
     k_scatter_ids<<<blocks_for(out.N, 256), 256, 0, st>>>(nc, out.N, noc.p);
     // 2. outputs in x-major order (the reference's node order, Subdomain.cpp:638-651)
     {
         int64_t* xg = nullptr;
         LBM_TRY(scan::compact(flags, npts, &xg, &out.NF, st));
-        out.node_grid.p = xg;
+        out.node_grid.adopt(xg, st);
         if (out.NF == 0) return fail(LBM_ERR_ARG, "instance %d has no fluid node", inst);
         DBuf<int32_t> rank;
-        LBM_TRY(rank.alloc(npts, "rank map"));
+        LBM_TRY(rank.alloc(npts, "rank map", st));
         k_scatter_ids<<<blocks_for(out.NF, 256), 256, 0, st>>>(xg, out.NF, rank.p);
-        LBM_TRY(out.out_pos.alloc(out.N, "output positions"));
+        LBM_TRY(out.out_pos.alloc(out.N, "output positions", st));
         k_out_pos<<<blocks_for(out.N, 256), 256, 0, st>>>(nc, out.N, type.p, D, P, rank.p, out_off, out.out_pos.p);
     }
     // 3. roles
     DBuf<int8_t> role;
-    LBM_TRY(role.alloc(out.N, "node roles"));
+    LBM_TRY(role.alloc(out.N, "node roles", st));
     k_roles_fluid<<<blocks_for(out.N, 256), 256, 0, st>>>(nc, out.N, type.p, role.p);
     const int64_t nb = geometry_nboundary(g);
     if (nb)
@@ -741,19 +783,19 @@ lbm_status build_instance(const lbm_geometry* g, const lbm_sim_params* p, int Q,
     uint64_t zl = 0;
     for (int l = 0; l < 64; ++l) if (kind[l] != LBM_BC_NONE) zl |= 1ull << l;
     DBuf<uint8_t> zf;
-    LBM_TRY(zf.alloc(out.N, "zou-he flags"));
+    LBM_TRY(zf.alloc(out.N, "zou-he flags", st));
     k_zflag<<<blocks_for(out.N, 256), 256, 0, st>>>(role.p, out.N, zl, zf.p);
     int64_t* zn = nullptr;
     int64_t nzn = 0;
     LBM_TRY(scan::compact(zf.p, out.N, &zn, &nzn, st));
-    DBuf<int64_t> znodes; znodes.p = zn;
+    DBuf<int64_t> znodes; znodes.adopt(zn, st);
     {
         // profile values follow the list's x-major order (the reference's
         // InletBoundaryNode_ order); slots follow the internal node order
         DBuf<int8_t> zr;
         DBuf<int32_t> zp;
-        LBM_TRY(zr.alloc(nzn, "zou-he roles"));
-        LBM_TRY(zp.alloc(nzn, "zou-he output positions"));
+        LBM_TRY(zr.alloc(nzn, "zou-he roles", st));
+        LBM_TRY(zp.alloc(nzn, "zou-he output positions", st));
         if (nzn)
             k_gather_role<<<blocks_for(nzn, 256), 256, 0, st>>>(zn, nzn, role.p, out.out_pos.p, zr.p, zp.p);
         std::vector<int8_t> hr(nzn);
@@ -798,15 +840,15 @@ lbm_status build_instance(const lbm_geometry* g, const lbm_sim_params* p, int Q,
     const int64_t ncol = (int64_t)D.Na * D.Nb;
     DBuf<int32_t> ccount, bcount;
     DBuf<int64_t> coff, moff;
-    LBM_TRY(ccount.alloc(ncol, "chunk counts"));
-    LBM_TRY(bcount.alloc(ncol, "boundary counts"));
-    LBM_TRY(coff.alloc(ncol, "chunk offsets"));
-    LBM_TRY(moff.alloc(ncol, "mask offsets"));
+    LBM_TRY(ccount.alloc(ncol, "chunk counts", st));
+    LBM_TRY(bcount.alloc(ncol, "boundary counts", st));
+    LBM_TRY(coff.alloc(ncol, "chunk offsets", st));
+    LBM_TRY(moff.alloc(ncol, "mask offsets", st));
     k_col_count<<<blocks_for(ncol, 128), 128, 0, st>>>(type.p, noc.p, role.p, D, ccount.p, bcount.p);
     LBM_TRY(scan::exclusive_scan(ccount.p, ncol, coff.p, &out.nchunks, st));
     LBM_TRY(scan::exclusive_scan(bcount.p, ncol, moff.p, &out.nmask, st));
-    LBM_TRY(out.chunks.alloc(out.nchunks, "chunks"));
-    LBM_TRY(out.mmask.alloc(out.nmask, "missing masks"));
+    LBM_TRY(out.chunks.alloc(out.nchunks, "chunks", st));
+    LBM_TRY(out.mmask.alloc(out.nmask, "missing masks", st));
     FillArgs fa;
     fa.type = type.p; fa.node_of_cell = noc.p; fa.role = role.p; fa.D = D; fa.V = make_vel(Q, ra);
     fa.chunk_off = coff.p; fa.mslot_off = moff.p;
@@ -820,10 +862,10 @@ lbm_status build_instance(const lbm_geometry* g, const lbm_sim_params* p, int Q,
         for (int k = 0; k < 3; ++k) {
             const int pc = 8 << k;
             DBuf<int64_t> coff2;
-            LBM_TRY(coff2.alloc(ncol, "paired chunk offsets"));
+            LBM_TRY(coff2.alloc(ncol, "paired chunk offsets", st));
             k_col_count2<<<blocks_for(ncol, 128), 128, 0, st>>>(type.p, D, pc, ccount.p);
             LBM_TRY(scan::exclusive_scan(ccount.p, ncol, coff2.p, &out.nchunks2[k], st));
-            LBM_TRY(out.chunks2[k].alloc(out.nchunks2[k], "paired chunks"));
+            LBM_TRY(out.chunks2[k].alloc(out.nchunks2[k], "paired chunks", st));
             FillArgs f2 = fa;
             f2.chunk_off = coff2.p;
             f2.chunks = out.chunks2[k].p;
@@ -1190,7 +1232,7 @@ lbm_status sim_create(const lbm_geometry* const* g, const lbm_sim_params* p, siz
     std::vector<double> wv(S->Q);
     for (int q = 0; q < S->Q; ++q) wv[q] = S->Q == 19 ? Lat<19>::w(q) : Lat<27>::w(q);
     DBuf<double> dw;
-    LBM_TRY(dw.alloc(S->Q, "weights"));
+    LBM_TRY(dw.alloc(S->Q, "weights", st));
     LBM_CUDA(cudaMemcpyAsync(dw.p, wv.data(), sizeof(double) * S->Q, cudaMemcpyHostToDevice, st));
     for (int b = 0; b < nb; ++b) {
         if (cudaMalloc(&S->buf[b], bytes) != cudaSuccess)
@@ -1228,7 +1270,7 @@ __global__ void k_gather_f64(const double* __restrict__ src, const int64_t* __re
 lbm_status sim_wall_positions(lbm_sim* S, const double* d_u, double* d_wss_pos, cudaStream_t st) {
     if (S->nwall >= 0) return LBM_OK;
     DBuf<uint8_t> flag;
-    LBM_TRY(flag.alloc(S->NF, "wall flags"));
+    LBM_TRY(flag.alloc(S->NF, "wall flags", st));
     LBM_CUDA(cudaMemsetAsync(flag.p, 0, S->NF, st));
     LBM_TRY(launch_wss(S->Q, S->ra, S->chunks, S->nchunks, S->mmask, S->out_pos, S->insts, d_u, d_wss_pos, flag.p, st));
     int64_t* idx = nullptr;
@@ -1559,9 +1601,9 @@ lbm_status lbm_sim_fields(lbm_sim* S, double* rho, double* u, double* f, size_t 
     clear_error();
     cudaStream_t st = (cudaStream_t)stream;
     DBuf<double> df, dr, du;
-    if (f) LBM_TRY(df.alloc((size_t)S->NF * S->Q, "field f"));
-    if (rho) LBM_TRY(dr.alloc(S->NF, "field rho"));
-    if (u) LBM_TRY(du.alloc((size_t)S->NF * 3, "field u"));
+    if (f) LBM_TRY(df.alloc((size_t)S->NF * S->Q, "field f", st));
+    if (rho) LBM_TRY(dr.alloc(S->NF, "field rho", st));
+    if (u) LBM_TRY(du.alloc((size_t)S->NF * 3, "field u", st));
     LBM_TRY(check_timeout(S, st));
     LBM_TRY(sim_dry(S, df.p, dr.p, du.p, false, st));
     if (f) LBM_CUDA(cudaMemcpyAsync(f, df.p, sizeof(double) * S->NF * S->Q, cudaMemcpyDeviceToHost, st));
@@ -1678,8 +1720,8 @@ lbm_status lbm_sim_wall_shear_stress(lbm_sim* S, double* wss, size_t cap, size_t
     clear_error();
     cudaStream_t st = (cudaStream_t)stream;
     DBuf<double> du, dpos, dw;
-    LBM_TRY(du.alloc((size_t)S->NF * 3, "velocity"));
-    LBM_TRY(dpos.alloc(S->NF, "wall shear stress"));
+    LBM_TRY(du.alloc((size_t)S->NF * 3, "velocity", st));
+    LBM_TRY(dpos.alloc(S->NF, "wall shear stress", st));
     LBM_TRY(check_timeout(S, st));
     LBM_TRY(sim_dry(S, nullptr, nullptr, du.p, false, st));
     LBM_TRY(sim_wall_positions(S, du.p, dpos.p, st));
@@ -1690,7 +1732,7 @@ lbm_status lbm_sim_wall_shear_stress(lbm_sim* S, double* wss, size_t cap, size_t
     }
     if (cap < (size_t)S->nwall) return fail(LBM_ERR_ARG, "lbm_sim_wall_shear_stress: capacity %zu < %lld wall nodes", cap,
                                             (long long)S->nwall);
-    LBM_TRY(dw.alloc(S->nwall, "wall shear stress"));
+    LBM_TRY(dw.alloc(S->nwall, "wall shear stress", st));
     LBM_TRY(sim_outputs(S, nullptr, du.p, dpos.p, dw.p, st));
     if (S->nwall) LBM_CUDA(cudaMemcpyAsync(wss, dw.p, sizeof(double) * S->nwall, cudaMemcpyDeviceToHost, st));
     LBM_CUDA(cudaStreamSynchronize(st));
@@ -1956,6 +1998,7 @@ lbm_status lbm_sim_restart(lbm_sim* S, const char* path, void* stream) {
 
 void lbm_sim_destroy(lbm_sim* S) {
     if (!S) return;
+    cudaDeviceSynchronize();               // pool memory (wall_pos) is freed without an implicit wait
     free_graph(S);
     for (void* b : S->buf) if (b) cudaFree(b);
     if (S->chunks) cudaFree(S->chunks);

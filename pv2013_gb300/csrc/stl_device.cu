@@ -166,6 +166,7 @@ struct ParseBufs {
     lbm_tri* tris = nullptr;
     int32_t* status = nullptr;
     ~ParseBufs() {
+        cudaDeviceSynchronize();           // ls, fl come from the stream-ordered pool: no implicit wait
         cudaFree(text);
         cudaFree(flags);
         cudaFree(ls);

@@ -360,12 +360,20 @@ class Simulation:
     def Iterate(self, n):
         self.step(n)
 
-    def fields(self, f=True, rho=True, u=True):
-        """FP64 host copies of f (N, Q), rho (N,), u (N, 3) of the current post-boundary state."""
+    def fields(self, f=True, rho=True, u=True, out=None):
+        """FP64 host copies of f (N, Q), rho (N,), u (N, 3) of the current post-boundary state.
+        ``out`` = (f, rho, u) caller-owned C-contiguous float64 arrays of those shapes (any may be None), e.g.
+        views of pinned host memory, written in place instead of new arrays."""
         n = self.info().n_nodes
-        fa = np.empty((n, self.Q)) if f else None
-        ra = np.empty(n) if rho else None
-        ua = np.empty((n, 3)) if u else None
+        if out is not None:
+            fa, ra, ua = out
+            for a, shape in ((fa, (n, self.Q)), (ra, (n,)), (ua, (n, 3))):
+                if a is not None and (a.dtype != np.float64 or a.shape != shape or not a.flags.c_contiguous):
+                    raise ValueError(f"fields: out array must be C-contiguous float64 of shape {shape}")
+        else:
+            fa = np.empty((n, self.Q)) if f else None
+            ra = np.empty(n) if rho else None
+            ua = np.empty((n, 3)) if u else None
         ptr = lambda a: a.ctypes.data_as(C.c_void_p) if a is not None else None  # noqa: E731
         check(load().lbm_sim_fields(self._h, ptr(ra), ptr(ua), ptr(fa), n, self._stream))
         return fa, ra, ua
