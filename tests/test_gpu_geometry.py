@@ -50,11 +50,48 @@ def test_full_bifurcation_matches_oracle(oracle_mod):
     _check_case(oracle_mod, cases.bifurcation())
 
 
+_TREE = {}
+
+
+def _tree_oracle(O):
+    """The benchmark's tree and its oracle geometry, computed once per session."""
+    if "geo" not in _TREE:
+        c = cases.vascular_tree(h=2.2)
+        _TREE["case"] = c
+        _TREE["geo"] = O.geometry(c.triangles, c.spacing, c.grid, c.predicates)
+    return _TREE["case"], _TREE["geo"]
+
+
 def test_full_vascular_tree_matches_oracle(oracle_mod):
     """The benchmark's vascular tree (512 x 1024 x 512 grid, 2.07 M triangles,
     32 outlet lists): node-type field, boundary points and every list bit-exact
     with the oracle (about a minute of OpenMP work on the host)."""
-    _check_case(oracle_mod, cases.vascular_tree(h=2.2))
+    c, geo = _tree_oracle(oracle_mod)
+    geom = c.geometry()
+    assert np.array_equal(geom.flags(), geo["flags"])
+    assert np.array_equal(geom.boundaryPoints, geo["bidx"])
+    assert np.array_equal(geom.WallboundaryPoints, geo["lists"]["wall"])
+    for lid in {p.list_id for p in c.predicates}:
+        assert np.array_equal(geom.list(lid), geo["lists"].get(lid, np.zeros(0, np.int64))), lid
+    assert geom.info.n_fluid == int(geo["flags"].sum())
+
+
+def test_full_vascular_tree_fp64_steps_bit_exact(oracle_mod):
+    """FP64 on the benchmark's tree itself (10.27 M fluid nodes, its inlet
+    with the parabolic profile and waveform, its outlets and walls): three AA
+    steps (even, odd, even launch), every population of every node bit-exact
+    with the oracle."""
+    from pv2013_gb300 import Simulation
+    O = oracle_mod
+    c, geo = _tree_oracle(O)
+    geom = c.geometry()
+    sim = Simulation(geom, c.tau, c.boundary_specs(geom), precision="f64", pattern="aa")
+    sim.step(3)
+    f = sim.fields(rho=False, u=False)[0]
+    del sim
+    ref = O.run_case(19, geo, c.tau, {0: (O.BC_VEL_NEGY, 1.0), 2: (O.BC_PRESS_POSY, c.outlet_rho)}, 3,
+                     profile=c.inlet_profile(geom), amp=c.amp_table())
+    assert np.array_equal(f, ref.f())
 
 
 def test_fine_spacing_matches_oracle(oracle_mod):
