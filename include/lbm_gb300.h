@@ -317,7 +317,9 @@ lbm_status lbm_sim_fields(lbm_sim* s, double* rho, double* u, double* f, size_t 
 /* rho and u as lbm_sim_fields gives them, for callers that must not allocate
  * device memory: the library writes them into one fixed device array of its
  * own (at most 524288 nodes; larger lattices: LBM_ERR_ARG) and copies them to
- * the caller's buffers, with no cudaMalloc or cudaFree.  The array is shared
+ * the caller's buffers, with no device allocation (neither the driver's
+ * allocator nor the library's memory pool, which lbm_sim_fields draws on
+ * and may grow).  The array is shared
  * by every call and keeps the last call's values, so calls whose GPU work
  * overlaps race.  The handle's device must be current.  The call
  * synchronises `stream` before it returns, so it cannot be used inside a

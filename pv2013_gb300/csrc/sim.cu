@@ -1616,12 +1616,13 @@ lbm_status lbm_sim_fields(lbm_sim* S, double* rho, double* u, double* f, size_t 
 // ---------------------------------------------------------------------------
 // Fields without device allocation (lbm_sim_fields_noalloc).
 //
-// lbm_sim_fields takes its FP64 output buffers from cudaMalloc and returns
-// them with cudaFree, and cudaFree waits until the whole device is idle.
-// Callers that sample rho and u while other work keeps the GPU busy -- a time
-// loop or another simulation running on other streams, a lattice sized to
-// fill the device memory, a process whose memory belongs to another
-// allocator -- cannot afford that wait or that allocation.  This variant runs
+// lbm_sim_fields takes its FP64 output buffers from the device's memory pool:
+// a call may grow the pool (a driver allocation, which can wait for the
+// device) and leaves that memory reserved for later calls.  Callers that
+// sample rho and u while other work keeps the GPU busy -- a time loop or
+// another simulation running on other streams, a lattice sized to fill the
+// device memory, a process whose memory belongs to another allocator --
+// cannot afford that wait or that allocation.  This variant runs
 // the same snapshot launch of the step kernel into one fixed device array
 // that is part of the library image, so a call allocates nothing.
 //
