@@ -23,9 +23,14 @@
 //     with one byte permute.  The AA odd launch runs on a piece table in
 //     which interior pieces come first within every 16-warp window
 //     (k_group_pieces, sim.cu), so most warps take no boundary branch.
+//   * descriptors: the AA even launch reads an 8-byte record per piece
+//     (n0, length and instance, a Zou-He flag; k_even_desc, sim.cu) and L2-
+//     prefetches the population windows of the piece half a wave ahead; the
+//     other launches read the 64-byte descriptor, the AA odd launch
+//     prefetching only the descriptor one wave ahead.
 // Chunk pieces start at even levels and hold up to 8, 16 or 32 node slots
 // (lbm_sim_params.piece_slots: shorter pieces leave fewer idle lanes where a
-// run ends, for 64 descriptor bytes per piece); a slot at either end may be a
+// run ends, for more descriptor bytes per node); a slot at either end may be a
 // ghost node (not in the piece's vmask): its values are computed and
 // discarded, and in the AA odd pattern it stores nothing.
 #pragma once
