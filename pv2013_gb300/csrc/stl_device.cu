@@ -159,6 +159,7 @@ unsigned grid_for(int64_t n, int threads) {
 
 // device buffers of one parse, released on every path
 struct ParseBufs {
+    cudaStream_t st = 0;
     char* text = nullptr;
     uint8_t* flags = nullptr;
     int64_t* ls = nullptr;
@@ -166,7 +167,7 @@ struct ParseBufs {
     lbm_tri* tris = nullptr;
     int32_t* status = nullptr;
     ~ParseBufs() {
-        cudaDeviceSynchronize();           // ls, fl come from the stream-ordered pool: no implicit wait
+        cudaStreamSynchronize(st);         // ls, fl come from the stream-ordered pool: no implicit wait
         cudaFree(text);
         cudaFree(flags);
         cudaFree(ls);
@@ -179,6 +180,7 @@ struct ParseBufs {
 lbm_status parse_on_device(const char* host_text, int64_t L, cudaStream_t st, lbm_tri** tris, size_t* n,
                            bool* ok) {
     ParseBufs B;
+    B.st = st;
     *ok = false;
     if (L == 0) {                           // no lines, no facets
         *tris = (lbm_tri*)std::malloc(sizeof(lbm_tri));
