@@ -370,6 +370,14 @@ lbm_status lbm_sim_set_wait_limit(lbm_sim* s, uint32_t polls);
  * such a step is incomplete; restore it (lbm_sim_restart) after disabling. */
 lbm_status lbm_sim_test_stall(lbm_sim* s, int32_t enable);
 
+/* Self-check hook (no counterpart in the reference): fills every population
+ * slot that belongs to no fluid node -- the ghost layer, the padding of the
+ * pair alignment, the slack at both ends of the arrays -- with NaN, in every
+ * plane of every lattice buffer.  No kernel may use such a value (a read of a
+ * ghost slot is a missing population, replaced by the boundary rule), so a
+ * correct build gives bit-identical results after it. */
+lbm_status lbm_sim_poison_ghosts(lbm_sim* s, void* stream);
+
 /* Converts the state to another streaming pattern (LBM_PULL or LBM_AA); the
  * run continues with the same results.  After an AA even (node-local)
  * launch the AA state is the pull state with its population planes

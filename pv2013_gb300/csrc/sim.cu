@@ -528,6 +528,19 @@ __global__ void k_even_desc(const Chunk* __restrict__ c, int64_t n, uint2* __res
     }
 }
 
+// NaN into every population slot of no fluid node (out_pos < 0, or beyond the
+// N lattice nodes): lbm_sim_poison_ghosts.  eb = bytes per stored value.
+__global__ void k_poison(void* a, int64_t stride, int Q, int eb, const int32_t* __restrict__ out_pos, int64_t N) {
+    const int64_t n = stride * Q;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t id = i % stride;
+        if (id < N && out_pos[id] >= 0) continue;
+        if (eb == 8) reinterpret_cast<uint64_t*>(a)[i] = 0x7ff8000000000000ull;
+        else if (eb == 4) reinterpret_cast<uint32_t*>(a)[i] = 0x7fc00000u;
+        else reinterpret_cast<uint16_t*>(a)[i] = 0x7fc0u;        // a quiet NaN in FP16 and in BF16
+    }
+}
+
 template <class T>
 __global__ void k_init_pop(T* __restrict__ a, int64_t stride, int Q, const double* __restrict__ val) {
     const int64_t n = stride * Q;
@@ -1707,6 +1720,19 @@ lbm_status lbm_sim_test_stall(lbm_sim* S, int32_t enable) {
     if (!S) return fail(LBM_ERR_ARG, "lbm_sim_test_stall: null handle");
     S->stall_first = enable ? 1 : 0;
     free_graph(S);
+    return LBM_OK;
+}
+
+lbm_status lbm_sim_poison_ghosts(lbm_sim* S, void* stream) {
+    if (!S) return fail(LBM_ERR_ARG, "lbm_sim_poison_ghosts: null handle");
+    clear_error();
+    cudaStream_t st = (cudaStream_t)stream;
+    const int eb = store_bytes(S->store);
+    for (void* b : S->buf)
+        if (b)
+            k_poison<<<blocks_for(S->stride * S->Q, 256), 256, 0, st>>>(b, S->stride, S->Q, eb, S->out_pos, S->N);
+    LBM_CUDA(cudaGetLastError());
+    LBM_CUDA(cudaStreamSynchronize(st));
     return LBM_OK;
 }
 

@@ -422,6 +422,10 @@ class Simulation:
         """Failure-test hook: the TMA-staged kernel's waits on each warp's first stage run out."""
         check(load().lbm_sim_test_stall(self._h, 1 if enable else 0))
 
+    def poison_ghosts(self):
+        """Self-check hook: NaN in every population slot of no fluid node (results must not change)."""
+        check(load().lbm_sim_poison_ghosts(self._h, self._stream))
+
     def wall_shear_stress(self):
         """Wall shear stress at every wall node, wall-list order (ComputeWallShearStress)."""
         lib = load()

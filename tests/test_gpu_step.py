@@ -249,3 +249,33 @@ def test_bounded_wait_runs_out_and_the_handle_recovers(tmp_path):
     sim.step(6)
     ref.step(6)
     assert np.array_equal(sim.fields()[0], ref.fields()[0])
+
+
+@pytest.mark.parametrize("precision,pattern,npl", [("f64", "pull", 1), ("f64", "aa", 1), ("f32", "pull", 2),
+                                                   ("f32", "aa", 1), ("f16s", "aa", 2), ("f16s", "pull", 2),
+                                                   ("bf16s", "aa", 2), ("f16s", "aa", 1)])
+def test_ghost_slots_never_reach_results(precision, pattern, npl):
+    """Self-check: NaN in every population slot of no fluid node (ghost layer,
+    pair padding, array slack), at the start and again mid-run, leaves every
+    population of every fluid node bit-identical and finite -- no kernel uses
+    a value it must replace (walls, inlet, outlet, graph replay included)."""
+    c = cases.vessel(4001)
+    c.inlet.period = 9
+    geom = c.geometry()
+    runs = []
+    for poison in (False, True):
+        sim = Simulation(geom, c.tau, c.boundary_specs(geom), precision=precision, pattern=pattern,
+                         nodes_per_lane=npl, staging=0 if npl == 1 else 1,
+                         corrections=_capi.FIX_LIST_NODES if pattern == "pull" else 0)
+        if poison:
+            sim.poison_ghosts()
+        sim.step(5)
+        if poison:
+            sim.poison_ghosts()
+        sim.step(8, graph=True)
+        f, rho, u = sim.fields()
+        mon = sim.monitors()
+        runs.append((f, mon))
+    (f0, m0), (f1, m1) = runs
+    assert np.isfinite(f1).all() and not m1["nonfinite"]
+    assert np.array_equal(f1, f0)
