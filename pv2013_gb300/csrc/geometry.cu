@@ -35,6 +35,7 @@
 #include "device.cuh"
 #include "internal.h"
 #include "scan.cuh"
+#include "nvtx.h"
 
 namespace lbm {
 
@@ -544,6 +545,7 @@ extern "C" {
 
 lbm_status lbm_geometry_create(const lbm_tri* tris, size_t ntris, double spacing, const lbm_grid* grid,
                                const lbm_bc_predicate* preds, size_t npreds, void* stream, lbm_geometry** out) {
+    const NvtxRange nvtx_range("lbm_geometry_create");
     if (!out || (!tris && ntris) || (!preds && npreds) || !(spacing > 0))
         return fail(LBM_ERR_ARG, "lbm_geometry_create: bad argument");
     clear_error();

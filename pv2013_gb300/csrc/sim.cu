@@ -30,6 +30,7 @@
 #include "device.cuh"
 #include "internal.h"
 #include "scan.cuh"
+#include "nvtx.h"
 #include "step.h"
 #include "step_kernel.cuh"
 
@@ -1352,6 +1353,7 @@ lbm_status snapshot_wait(lbm_snapshot* P) {
 extern "C" {
 
 lbm_status lbm_sim_create(const lbm_geometry* g, const lbm_sim_params* p, void* stream, lbm_sim** out) {
+    const NvtxRange nvtx_range("lbm_sim_create");
     if (!g || !p || !out) return fail(LBM_ERR_ARG, "lbm_sim_create: null argument");
     clear_error();
     *out = nullptr;
@@ -1364,6 +1366,7 @@ lbm_status lbm_sim_create(const lbm_geometry* g, const lbm_sim_params* p, void* 
 
 lbm_status lbm_batch_create(const lbm_geometry* const* g, const lbm_sim_params* p, size_t n, void* stream,
                             lbm_sim** out) {
+    const NvtxRange nvtx_range("lbm_batch_create");
     if (!g || !p || !out || n == 0) return fail(LBM_ERR_ARG, "lbm_batch_create: bad argument");
     if (n >= (1u << 24)) return fail(LBM_ERR_ARG, "lbm_batch_create: too many instances");
     clear_error();
@@ -1376,6 +1379,7 @@ lbm_status lbm_batch_create(const lbm_geometry* const* g, const lbm_sim_params* 
 }
 
 lbm_status lbm_sim_step(lbm_sim* S, int64_t nsteps, uint32_t flags, void* stream) {
+    const NvtxRange nvtx_range("lbm_sim_step");
     if (!S || nsteps < 0) return fail(LBM_ERR_ARG, "lbm_sim_step: bad argument");
     // the kernels take the inlet waveform phase from a 32-bit step count
     if (S->steps_done + nsteps > (int64_t)0xffffffffLL)
@@ -1482,6 +1486,7 @@ static lbm_status convert_pattern(lbm_sim* S, int pattern, cudaStream_t st) {
 }
 
 lbm_status lbm_sim_set_pattern(lbm_sim* S, int32_t pattern, void* stream) {
+    const NvtxRange nvtx_range("lbm_sim_set_pattern");
     if (!S || (pattern != LBM_PULL && pattern != LBM_AA)) return fail(LBM_ERR_ARG, "lbm_sim_set_pattern: bad argument");
     clear_error();
     LBM_TRY(check_timeout(S, (cudaStream_t)stream));
@@ -1490,6 +1495,7 @@ lbm_status lbm_sim_set_pattern(lbm_sim* S, int32_t pattern, void* stream) {
 
 lbm_status lbm_sim_autotune(lbm_sim* S, int32_t launches, void* stream, lbm_tune_entry* entries, size_t cap,
                             size_t* n) {
+    const NvtxRange nvtx_range("lbm_sim_autotune");
     if (!S || launches < 2) return fail(LBM_ERR_ARG, "lbm_sim_autotune: null handle or fewer than 2 launches");
     clear_error();
     cudaStream_t st = (cudaStream_t)stream;
@@ -1609,6 +1615,7 @@ lbm_status lbm_sim_info_get(const lbm_sim* S, lbm_sim_info* info) {
 }
 
 lbm_status lbm_sim_fields(lbm_sim* S, double* rho, double* u, double* f, size_t n_nodes, void* stream) {
+    const NvtxRange nvtx_range("lbm_sim_fields");
     if (!S) return fail(LBM_ERR_ARG, "lbm_sim_fields: null handle");
     if (n_nodes < (size_t)S->NF) return fail(LBM_ERR_ARG, "lbm_sim_fields: capacity %zu < %lld nodes", n_nodes, (long long)S->NF);
     clear_error();
@@ -1704,6 +1711,7 @@ lbm_status lbm_sim_instance_offsets(const lbm_sim* S, int64_t* off, size_t cap) 
 }
 
 lbm_status lbm_sim_monitors(lbm_sim* S, lbm_monitors* out, void* stream) {
+    const NvtxRange nvtx_range("lbm_sim_monitors");
     if (!S || !out) return fail(LBM_ERR_ARG, "lbm_sim_monitors: null argument");
     clear_error();
     return sim_monitors(S, out, (cudaStream_t)stream);
@@ -1743,6 +1751,7 @@ lbm_status lbm_sim_set_divergence_tolerance(lbm_sim* S, double rel_tol) {
 }
 
 lbm_status lbm_sim_wall_shear_stress(lbm_sim* S, double* wss, size_t cap, size_t* n, void* stream) {
+    const NvtxRange nvtx_range("lbm_sim_wall_shear_stress");
     if (!S) return fail(LBM_ERR_ARG, "lbm_sim_wall_shear_stress: null handle");
     clear_error();
     cudaStream_t st = (cudaStream_t)stream;
@@ -1955,6 +1964,7 @@ constexpr size_t kCkptBlock = size_t(64) << 20;
 }  // namespace
 
 lbm_status lbm_sim_checkpoint(lbm_sim* S, const char* path, void* stream) {
+    const NvtxRange nvtx_range("lbm_sim_checkpoint");
     if (!S || !path) return fail(LBM_ERR_ARG, "lbm_sim_checkpoint: null argument");
     clear_error();
     cudaStream_t st = (cudaStream_t)stream;
@@ -1980,6 +1990,7 @@ lbm_status lbm_sim_checkpoint(lbm_sim* S, const char* path, void* stream) {
 }
 
 lbm_status lbm_sim_restart(lbm_sim* S, const char* path, void* stream) {
+    const NvtxRange nvtx_range("lbm_sim_restart");
     if (!S || !path) return fail(LBM_ERR_ARG, "lbm_sim_restart: null argument");
     clear_error();
     cudaStream_t st = (cudaStream_t)stream;
