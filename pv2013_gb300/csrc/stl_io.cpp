@@ -9,7 +9,9 @@
 // are converted with strtod, which rounds correctly like the reference's
 // istream >> double; tokens istream rejects (nan, inf, out of range) are
 // rejected here too.
+#include <algorithm>
 #include <cerrno>
+#include <new>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -117,9 +119,19 @@ const char* lbm_status_string(lbm_status s) {
 void lbm_free(void* p) { std::free(p); }
 int lbm_abi_version(void) { return LBM_ABI_VERSION; }
 
+static lbm_status read_ascii(const char* path, lbm_tri** tris, size_t* n);
+
 lbm_status lbm_stl_read_ascii(const char* path, lbm_tri** tris, size_t* n) {
     if (!path || !tris || !n) return fail(LBM_ERR_ARG, "lbm_stl_read_ascii: null argument");
     clear_error();
+    try {
+        return read_ascii(path, tris, n);
+    } catch (const std::bad_alloc&) {               // no exception crosses the C ABI
+        return fail(LBM_ERR_NOMEM, "%s: out of host memory", path);
+    }
+}
+
+static lbm_status read_ascii(const char* path, lbm_tri** tris, size_t* n) {
     std::ifstream file(path);
     if (!file.is_open()) return fail(LBM_ERR_IO, "cannot open file %s", path);
     TriVec out;
@@ -174,19 +186,29 @@ lbm_status lbm_stl_read_binary(const char* path, lbm_tri** tris, size_t* n) {
     uint32_t count = 0;
     if (!file.read(header, 80) || !file.read(reinterpret_cast<char*>(&count), 4))
         return fail(LBM_ERR_PARSE, "%s: truncated binary STL header", path);
+    // the facet count is the file's claim: reserve no more than the bytes
+    // after the header can hold (a corrupt count must not allocate for it)
+    const std::streampos here = file.tellg();
+    file.seekg(0, std::ios::end);
+    const std::streamoff left = file.tellg() - here;
+    file.seekg(here);
     TriVec out;
-    out.reserve(count);
-    for (uint32_t i = 0; i < count; ++i) {
-        float v[12];
-        uint16_t attr;
-        if (!file.read(reinterpret_cast<char*>(v), 48) || !file.read(reinterpret_cast<char*>(&attr), 2))
-            return fail(LBM_ERR_PARSE, "%s: truncated at facet %u of %u", path, i, count);
-        // normal first in the file; renormalised in float (GeometryReader.cpp:138-141)
-        float nx = v[0], ny = v[1], nz = v[2];
-        float norm = std::sqrt(nx * nx + ny * ny + nz * nz);
-        nx /= norm; ny /= norm; nz /= norm;
-        lbm_tri t = {v[3], v[4], v[5], v[6], v[7], v[8], v[9], v[10], v[11], nx, ny, nz};
-        out.push_back(t);
+    try {
+        out.reserve(std::min<uint64_t>(count, left > 0 ? (uint64_t)left / 50 : 0));
+        for (uint32_t i = 0; i < count; ++i) {
+            float v[12];
+            uint16_t attr;
+            if (!file.read(reinterpret_cast<char*>(v), 48) || !file.read(reinterpret_cast<char*>(&attr), 2))
+                return fail(LBM_ERR_PARSE, "%s: truncated at facet %u of %u", path, i, count);
+            // normal first in the file; renormalised in float (GeometryReader.cpp:138-141)
+            float nx = v[0], ny = v[1], nz = v[2];
+            float norm = std::sqrt(nx * nx + ny * ny + nz * nz);
+            nx /= norm; ny /= norm; nz /= norm;
+            lbm_tri t = {v[3], v[4], v[5], v[6], v[7], v[8], v[9], v[10], v[11], nx, ny, nz};
+            out.push_back(t);
+        }
+    } catch (const std::bad_alloc&) {
+        return fail(LBM_ERR_NOMEM, "%s: out of host memory for %u facets", path, count);
     }
     return to_c_array(out, tris, n);
 }
