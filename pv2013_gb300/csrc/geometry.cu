@@ -554,7 +554,8 @@ lbm_status lbm_geometry_create(const lbm_tri* tris, size_t ntris, double spacing
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(LBM_ERR_NODEV, "no CUDA device");
     lbm_geometry* G = new lbm_geometry();
     cudaGetDevice(&G->dev);
-    lbm_status s = geometry_build(G, tris, ntris, spacing, grid, preds, npreds, (cudaStream_t)stream);
+    lbm_status s = guarded("lbm_geometry_create",
+                           [&] { return geometry_build(G, tris, ntris, spacing, grid, preds, npreds, (cudaStream_t)stream); });
     if (s != LBM_OK) { lbm_geometry_destroy(G); return s; }
     *out = G;
     return LBM_OK;

@@ -4,6 +4,8 @@
 #include <cstdarg>
 #include <cstdint>
 #include <cstdio>
+#include <exception>
+#include <new>
 #include <string>
 #include <vector>
 
@@ -22,6 +24,20 @@ void clear_error();
 // for the device: callers synchronise first.
 lbm_status dev_alloc(void** p, size_t bytes, void* stream, const char* what);
 void dev_free(void* p, void* stream);
+
+// Runs f (returning lbm_status) so that no C++ exception crosses the C ABI:
+// an allocation failure becomes LBM_ERR_NOMEM, any other exception
+// LBM_ERR_STATE with its message.
+template <class F>
+lbm_status guarded(const char* what, F&& f) {
+    try {
+        return f();
+    } catch (const std::bad_alloc&) {
+        return fail(LBM_ERR_NOMEM, "%s: out of host memory", what);
+    } catch (const std::exception& e) {
+        return fail(LBM_ERR_STATE, "%s: %s", what, e.what());
+    }
+}
 
 // Triangle array helpers (host).
 using TriVec = std::vector<lbm_tri>;

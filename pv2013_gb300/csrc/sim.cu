@@ -1358,7 +1358,7 @@ lbm_status lbm_sim_create(const lbm_geometry* g, const lbm_sim_params* p, void* 
     clear_error();
     *out = nullptr;
     lbm_sim* S = nullptr;
-    lbm_status s = sim_create(&g, p, 1, (cudaStream_t)stream, &S);
+    lbm_status s = guarded("lbm_sim_create", [&] { return sim_create(&g, p, 1, (cudaStream_t)stream, &S); });
     if (s != LBM_OK) return s;
     *out = S;
     return LBM_OK;
@@ -1372,7 +1372,7 @@ lbm_status lbm_batch_create(const lbm_geometry* const* g, const lbm_sim_params* 
     clear_error();
     *out = nullptr;
     lbm_sim* S = nullptr;
-    lbm_status s = sim_create(g, p, n, (cudaStream_t)stream, &S);
+    lbm_status s = guarded("lbm_batch_create", [&] { return sim_create(g, p, n, (cudaStream_t)stream, &S); });
     if (s != LBM_OK) return s;
     *out = S;
     return LBM_OK;

@@ -239,10 +239,12 @@ lbm_status lbm_synth_capsules(const double* seg, size_t nseg, const double lo[3]
                               uint64_t seed, lbm_tri** tris, size_t* n) {
     if (!seg || !lo || !hi || !tris || !n) return fail(LBM_ERR_ARG, "lbm_synth_capsules: null argument");
     clear_error();
-    TriVec out;
-    lbm_status st = mesh_capsules(seg, nseg, lo, hi, h, seed, out);
-    if (st != LBM_OK) return st;
-    return to_c_array(out, tris, n);
+    return guarded("lbm_synth_capsules", [&] {
+        TriVec out;
+        lbm_status st = mesh_capsules(seg, nseg, lo, hi, h, seed, out);
+        if (st != LBM_OK) return st;
+        return to_c_array(out, tris, n);
+    });
 }
 
 }  // extern "C"
