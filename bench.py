@@ -439,7 +439,9 @@ def gpu_arm(args, rank, world):
                 "d2h_bytes_per_step": d2h / e2e_steps,
                 "includes": "STL triangles H2D from pinned host memory, GPU voxelization, lattice build, steps, rho/u D2H into pinned host memory",
                 "parts": e2e_parts},
-        "gpu_launches": args.steps + args.steps // 64 + 2,
+        # kernels of the timed region: graphs of 64 step launches plus the
+        # step-counter update, then the remaining steps as direct launches
+        "gpu_launches": (args.steps // 64) * 65 + args.steps % 64,
         "voxelize_ms": geom.info.voxelize_ms, "mesh_s": t_mesh,
         "clocks": clk.summary(), "monitors_after": {k: mon[k] for k in ("mass", "max_speed", "nonfinite")},
     }
