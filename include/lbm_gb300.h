@@ -273,6 +273,11 @@ lbm_status lbm_batch_create(const lbm_geometry* const* g, const lbm_sim_params* 
 #define LBM_STEP_GRAPH 1u      /* replay the steps as a captured CUDA graph */
 #define LBM_STEP_MONITOR 2u    /* run the divergence monitor after the last step */
 lbm_status lbm_sim_step(lbm_sim* s, int64_t nsteps, uint32_t flags, void* stream);
+/* Captures now the CUDA graph a later lbm_sim_step(s, nsteps, LBM_STEP_GRAPH)
+ * from the current state replays (at most 64 launches long), so that call
+ * spends no time on the capture.  The state does not change; a call with
+ * another step count may capture again.  No counterpart in the reference. */
+lbm_status lbm_sim_prepare_graph(lbm_sim* s, int64_t nsteps, void* stream);
 
 typedef struct lbm_sim_info {
     int64_t n_nodes;

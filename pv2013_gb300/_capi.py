@@ -142,6 +142,7 @@ PROTOTYPES = {
     "lbm_sim_set_wait_limit": (C.c_int, [C.c_void_p, C.c_uint32]),
     "lbm_sim_test_stall": (C.c_int, [C.c_void_p, C.c_int32]),
     "lbm_sim_poison_ghosts": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "lbm_sim_prepare_graph": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p]),
     "lbm_sim_set_pattern": (C.c_int, [C.c_void_p, C.c_int32, C.c_void_p]),
     "lbm_sim_destroy": (None, [C.c_void_p]),
     "lbm_synth_cylinder": (C.c_int, [C.c_double, C.c_double, C.c_int32, C.c_int32, _P(C.c_double),

@@ -1378,6 +1378,64 @@ lbm_status lbm_batch_create(const lbm_geometry* const* g, const lbm_sim_params* 
     return LBM_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// The CUDA graph of G launches (G even) from an aligned state (pull: the
+// first buffer is the source; AA: an even, node-local launch first), plus the
+// step-counter update; captured once per length.  The simulation's state is
+// untouched: the graph's launches take their step numbers from step_base.
+lbm_status ensure_graph(lbm_sim* S, int64_t G) {
+    if (S->glen == G) return LBM_OK;
+    free_graph(S);
+    cudaStream_t cs;
+    LBM_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    const int cur0 = S->cur;
+    const int64_t sd0 = S->steps_done;
+    // aligned state for the capture (restored below)
+    S->cur = 0;
+    S->steps_done = sd0 + ((sd0 + S->aa_phase) & 1);
+    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    lbm_status ls = LBM_OK;
+    for (int64_t s = 0; s < G && ls == LBM_OK && e == cudaSuccess; ++s) {
+        ls = sim_one_step(S, s, S->step_base, cs, false);
+        S->steps_done++;   // parity for AA within the capture
+    }
+    if (e == cudaSuccess) {
+        k_add_step<<<1, 1, 0, cs>>>(S->step_base, G);
+        e = cudaStreamEndCapture(cs, &S->graph);
+    }
+    S->cur = cur0;
+    S->steps_done = sd0;
+    cudaStreamDestroy(cs);
+    if (ls != LBM_OK) return ls;
+    if (e != cudaSuccess) return fail(LBM_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+    LBM_CUDA(cudaGraphInstantiate(&S->gexec, S->graph, 0));
+    S->glen = G;
+    return LBM_OK;
+}
+
+// graph length lbm_sim_step uses for nsteps from the current state (0: none)
+int64_t graph_length(const lbm_sim* S, int64_t nsteps) {
+    if (nsteps < 4) return 0;
+    const bool misaligned = S->pattern == LBM_PULL ? S->cur != 0 : aa_mode(S) != MODE_AA_EVEN;
+    const int64_t G = std::min<int64_t>(64, (nsteps - (misaligned ? 1 : 0)) & ~1LL);
+    return G >= 2 ? G : 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+lbm_status lbm_sim_prepare_graph(lbm_sim* S, int64_t nsteps, void* stream) {
+    if (!S || nsteps < 0) return fail(LBM_ERR_ARG, "lbm_sim_prepare_graph: bad argument");
+    clear_error();
+    (void)stream;
+    const int64_t G = graph_length(S, nsteps);
+    return G ? ensure_graph(S, G) : LBM_OK;
+}
+
 lbm_status lbm_sim_step(lbm_sim* S, int64_t nsteps, uint32_t flags, void* stream) {
     const NvtxRange nvtx_range("lbm_sim_step");
     if (!S || nsteps < 0) return fail(LBM_ERR_ARG, "lbm_sim_step: bad argument");
@@ -1387,44 +1445,21 @@ lbm_status lbm_sim_step(lbm_sim* S, int64_t nsteps, uint32_t flags, void* stream
     clear_error();
     cudaStream_t st = (cudaStream_t)stream;
     int64_t left = nsteps;
-    if ((flags & LBM_STEP_GRAPH) && nsteps >= 4) {
+    const int64_t G = (flags & LBM_STEP_GRAPH) ? graph_length(S, nsteps) : 0;
+    if (G) {
         // state parity must match the captured graph: pull buffer index and
         // AA step parity both return to their start after an even step count
         if (S->pattern == LBM_PULL ? S->cur != 0 : aa_mode(S) != MODE_AA_EVEN) {
             LBM_TRY(sim_one_step(S, S->steps_done, nullptr, st, true));
             --left;
         }
-        const int64_t G = std::min<int64_t>(64, left & ~1LL);
-        if (G >= 2) {
-            if (S->glen != G) {
-                free_graph(S);
-                cudaStream_t cs;
-                LBM_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
-                LBM_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-                const int cur0 = S->cur;
-                const int64_t sd0 = S->steps_done;
-                lbm_status ls = LBM_OK;
-                for (int64_t s = 0; s < G && ls == LBM_OK; ++s) {
-                    ls = sim_one_step(S, s, S->step_base, cs, false);
-                    S->steps_done++;   // parity for AA within the capture
-                }
-                k_add_step<<<1, 1, 0, cs>>>(S->step_base, G);
-                cudaError_t e = cudaStreamEndCapture(cs, &S->graph);
-                S->cur = cur0;
-                S->steps_done = sd0;
-                cudaStreamDestroy(cs);
-                if (ls != LBM_OK) return ls;
-                if (e != cudaSuccess) return fail(LBM_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
-                LBM_CUDA(cudaGraphInstantiate(&S->gexec, S->graph, 0));
-                S->glen = G;
-            }
-            int64_t sd = S->steps_done;
-            LBM_CUDA(cudaMemcpyAsync(S->step_base, &sd, sizeof sd, cudaMemcpyHostToDevice, st));
-            while (left >= G) {
-                LBM_CUDA(cudaGraphLaunch(S->gexec, st));
-                S->steps_done += G;
-                left -= G;
-            }
+        LBM_TRY(ensure_graph(S, G));
+        int64_t sd = S->steps_done;
+        LBM_CUDA(cudaMemcpyAsync(S->step_base, &sd, sizeof sd, cudaMemcpyHostToDevice, st));
+        while (left >= G) {
+            LBM_CUDA(cudaGraphLaunch(S->gexec, st));
+            S->steps_done += G;
+            left -= G;
         }
     }
     for (; left > 0; --left) LBM_TRY(sim_one_step(S, S->steps_done, nullptr, st, true));

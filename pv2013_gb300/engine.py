@@ -356,6 +356,10 @@ class Simulation:
         flags = (_capi.STEP_GRAPH if graph else 0) | (_capi.STEP_MONITOR if monitor else 0)
         check(load().lbm_sim_step(self._h, int(n), flags, self._stream))
 
+    def prepare_graph(self, n):
+        """Captures the CUDA graph that step(n, graph=True) from the current state replays."""
+        check(load().lbm_sim_prepare_graph(self._h, int(n), self._stream))
+
     # reference spelling: Simulation::Iterate runs the time loop
     def Iterate(self, n):
         self.step(n)

@@ -279,3 +279,24 @@ def test_ghost_slots_never_reach_results(precision, pattern, npl):
     (f0, m0), (f1, m1) = runs
     assert np.isfinite(f1).all() and not m1["nonfinite"]
     assert np.array_equal(f1, f0)
+
+
+@pytest.mark.parametrize("pattern", ["pull", "aa"])
+@pytest.mark.parametrize("precision", ["f64", "f16s"])
+def test_prepared_graph_equals_direct_steps(pattern, precision):
+    """A graph captured ahead (lbm_sim_prepare_graph), from an aligned and
+    from a misaligned state, replays the same steps as direct launches."""
+    c = cases.vessel(4001)
+    c.inlet.period = 9
+    geom = c.geometry()
+    a = Simulation(geom, c.tau, c.boundary_specs(geom), precision=precision, pattern=pattern)
+    b = Simulation(geom, c.tau, c.boundary_specs(geom), precision=precision, pattern=pattern)
+    a.step(3)                       # misaligned: the replay starts with one direct step
+    f3 = a.fields()[0]
+    a.prepare_graph(70)
+    assert a.info().steps_done == 3 and np.array_equal(a.fields()[0], f3)   # the state is untouched
+    a.step(70, graph=True)
+    a.prepare_graph(40)
+    a.step(40, graph=True)
+    b.step(113)
+    assert np.array_equal(a.fields()[0], b.fields()[0])
